@@ -1,0 +1,425 @@
+"""Benchmark of the GB300 MSM engine (BLS12-377 G1) -- one JSON line on rank 0.
+
+Workload (the largest single-GPU plain configuration): one MSM of N = 2^24 seeded bases
+k_i * G (resident in HBM in precomputed twisted-Edwards form) with uniform 253-bit scalars per
+step.  Inputs are synthetic and seeded; scalar and base buffers (512 MB + 2.4 GB) exceed the
+129 MB L2, so no flush is needed between steps.
+
+  value  MSMs/s with the step's scalars already in device memory (msm_mult_device)
+  e2e    MSMs/s through msm_mult with host scalars: H2D of 32 B per point and D2H of the
+         144-byte result inside the timed region
+  extra  points/s, per-step p50/p99, the uneven batch (64 MSMs of 2^10..2^20 over a shared 2^20
+         base set: one pass with a shared sort replayed from a CUDA graph vs one pass per MSM),
+         the served mix (Poisson arrivals, sizes 2^12..2^22 over a 2^22 base set) and the
+         oracle port timed on the host cores.
+
+`--impl reference` times the CPU port of the reference's oracle algorithm (arkworks-style
+Pippenger, oracle/cpu_msm.c) on all host cores on the same workload; the reference itself
+(OCaml RTL + XRT host, Rust/arkworks harness) cannot run on this machine.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+C_MADD = 4116   # 7 Montgomery products x 588 IMAD (12 x 32-bit limbs)
+C_ADD = 5292    # 9 products
+
+
+def imad_model(n: int, c: int) -> float:
+    w = math.ceil(253 / c)
+    return n * w * C_MADD + w * 2 ** (c - 1) * 2 * C_ADD + 253 * C_ADD + w * C_ADD
+
+
+def algorithmic_imad(n: int) -> float:
+    """A(N) = min over c in 10..16 of the IMAD count of a signed-window Pippenger."""
+    return min(imad_model(n, c) for c in range(10, 17))
+
+
+# ---------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def percentile(v, p):
+    s = sorted(v)
+    k = min(len(s) - 1, max(0, int(math.ceil(p / 100.0 * len(s))) - 1))
+    return s[k]
+
+
+# ---------------------------------------------------------------------------------------------
+def cpu_msm_time(points, scalars, threads):
+    from oracle import cpu as ocpu
+    t0 = time.perf_counter()
+    out = ocpu.msm(points, scalars, threads=threads)
+    return time.perf_counter() - t0, out
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the CPU port of the oracle algorithm on all host cores."""
+    if rank != 0:
+        return
+    import hardcaml_zprize_gb300 as eng
+    from oracle import cpu as ocpu
+    n = 1 << args.log2n
+    cores = os.cpu_count() or 1
+    pts = ocpu.gen_bases(args.seed, n, threads=cores)
+    sc = eng.generate_scalars(args.seed + 1, n)
+    for _ in range(args.warmup):
+        cpu_msm_time(pts, sc, cores)
+    times = [cpu_msm_time(pts, sc, cores)[0] for _ in range(args.steps)]
+    t = sum(times)
+    v = args.steps / t
+    line = {
+        "impl": "reference", "metric": "msm_per_s", "value": v, "unit": "MSM/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
+        "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n},
+        "cpu_baseline": {"value": v, "unit": "MSM/s", "cores": cores, "kind": "port",
+                         "sample": f"one full MSM of 2^{args.log2n} points per step"},
+        "e2e": {"value": v, "unit": "MSM/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "points_per_s": v * n,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import hardcaml_zprize_gb300 as eng
+    from hardcaml_zprize_gb300 import build
+    build.build()
+    import torch
+
+    n = 1 << args.log2n
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    os.environ["MSM_DEVICE"] = str(local)
+    info = eng.device_info()
+    peak_imad = eng.measure_imad_peak()
+
+    # ---- data: seeded bases on the GPU, scalars on the host ----
+    t0 = time.perf_counter()
+    pts = eng.generate_bases(args.seed, n)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx = eng.multi_scalar_mult_init(pts)
+    t_init = time.perf_counter() - t0
+    nsteps = args.steps + args.warmup
+    host_sc = [eng.generate_scalars(args.seed + 1 + rank * 1000 + s, n) for s in range(min(nsteps, 2))]
+    dev_sc = [torch.from_numpy(h.view(np.uint8).reshape(-1)).to(dev) for h in host_sc]
+    torch.cuda.synchronize()
+
+    sizes, offs = [n], [0]
+
+    def step_device(i):
+        return ctx.mult_device(sizes, offs, dev_sc[i % len(dev_sc)].data_ptr())
+
+    # ---- value: resident inputs ----
+    for i in range(args.warmup):
+        step_device(i)
+    lat = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            s0 = time.perf_counter()
+            step_device(i)
+            lat.append(time.perf_counter() - s0)
+        torch.cuda.synchronize()
+        t_dev = time.perf_counter() - t0
+    barrier(world)
+    t_dev = max_over_ranks(t_dev, world)
+    clocks = clk.summary()
+
+    # ---- per-stage timing (CUDA events on the pipeline stream), separate pass ----
+    ctx.set_timing(True)
+    stage_acc = {}
+    reps = max(2, min(args.steps, 5))
+    for i in range(reps):
+        step_device(i)
+        for k, v in ctx.last_timings().items():
+            stage_acc[k] = stage_acc.get(k, 0.0) + v / reps
+    stats = ctx.last_pass_stats()
+    ctx.set_timing(False)
+    cfg = ctx.config(n)
+
+    # ---- e2e: host scalars through msm_mult ----
+    for i in range(args.warmup):
+        eng.multi_scalar_mult(ctx, pts, host_sc[i % len(host_sc)])
+    barrier(world)
+    t0 = time.perf_counter()
+    last = None
+    for i in range(args.steps):
+        last = eng.multi_scalar_mult(ctx, pts, host_sc[i % len(host_sc)])
+    t_e2e = time.perf_counter() - t0
+    barrier(world)
+    t_e2e = max_over_ranks(t_e2e, world)
+
+    value = world * args.steps / t_dev
+    e2e = world * args.steps / t_e2e
+    ms_per_step = 1e3 * t_dev / args.steps
+    msm_s = t_dev / args.steps
+    t_acc = stage_acc.get("accumulate", 0) * 1e-3
+    w_used = math.ceil(253 / cfg["window_bits"])
+    acc_imad = n * w_used * C_MADD
+    achieved = acc_imad / t_acc if t_acc > 0 else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "k_accumulate_traffic.json")
+    if os.path.exists(tf):
+        try:
+            tr = json.load(open(tf))
+            traffic = tr["bytes_per_point_window"] * n * w_used
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "msm_per_s", "value": value, "unit": "MSM/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
+        "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n,
+                   "l2": "inputs larger than L2 (512 MB scalars, 2.4 GB bases)",
+                   "window_bits": cfg["window_bits"], "signed_digits": cfg["signed_digits"] == 1,
+                   "seg_len": cfg["seg_len"], "red_len_log2": cfg["red_len_log2"]},
+        "e2e": {"value": e2e, "unit": "MSM/s", "h2d_bytes_per_step": n * 32,
+                "d2h_bytes_per_step": 144},
+        "gpu_launches": 11 * args.steps,
+        "points_per_s": value * n,
+        "latency_ms": {"p50": 1e3 * percentile(lat, 50), "p99": 1e3 * percentile(lat, 99)},
+        "roofline": {
+            "bound": "imad", "kernel": "k_accumulate",
+            "achieved": achieved / 1e12 if achieved else None, "peak": peak_imad / 1e12,
+            "unit": "TIMAD/s", "frac": (achieved / peak_imad) if achieved else None,
+            "traffic": traffic,
+            "algorithmic_imad_per_launch": acc_imad,
+            "peak_source": "measured in this run: msm_measure_imad_peak (independent mad.lo/mad.hi "
+                           "chains on all SMs)",
+            "msm_achieved": algorithmic_imad(n) / msm_s / 1e12,
+            "msm_frac": algorithmic_imad(n) / msm_s / peak_imad,
+        },
+        "stages_ms": stage_acc,
+        "pass_stats": stats,
+        "clocks": clocks,
+        "device": info,
+        "setup_s": {"generate_bases": t_gen, "msm_init": t_init},
+    }
+
+    # ---- uneven batch: batched (one pass, shared sort, graph) vs plain (one pass per MSM) ----
+    if not args.skip_batched and rank == 0:
+        line["batched"] = bench_batched(args, eng, ctx, torch, dev)
+    # ---- served mix ----
+    if not args.skip_served and rank == 0:
+        line["served"] = bench_served(args, eng, ctx, n)
+    # ---- CPU baseline on the host cores, plus a bit-exact check of the GPU result ----
+    if not args.skip_cpu and rank == 0:
+        cores = os.cpu_count() or 1
+        t_cpu, out_cpu = cpu_msm_time(pts, host_sc[(args.steps - 1) % len(host_sc)], cores)
+        line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "MSM/s", "cores": cores, "kind": "port",
+                                "sample": f"one full MSM of 2^{args.log2n} points (oracle/cpu_msm.c, "
+                                          f"arkworks-0.3-style Pippenger, OpenMP over windows)"}
+        line["parity_vs_cpu"] = bool(np.array_equal(last[0], out_cpu))
+        line["speedup_vs_cpu"] = {"value": value * t_cpu, "e2e": e2e * t_cpu}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def bench_batched(args, eng, ctx, torch, dev):
+    rng = np.random.default_rng(args.seed + 7)
+    nbase = 1 << 20
+    m = 64
+    sizes = [int(2 ** u) for u in rng.uniform(10, 20, m)]
+    offs = [int(rng.integers(0, nbase - s + 1)) for s in sizes]
+    sc = np.concatenate([eng.generate_scalars(args.seed + 11, s, kind=1, msm_index=j)
+                         for j, s in enumerate(sizes)])
+    dsc = torch.from_numpy(sc.view(np.uint8).reshape(-1)).to(dev)
+    torch.cuda.synchronize()
+    res = {}
+    outs = {}
+    for name, opts in (("plain", dict(mode=1)), ("batched", dict(mode=2, use_graph=1))):
+        for _ in range(max(args.warmup, 2)):
+            outs[name] = ctx.mult_device(sizes, offs, dsc.data_ptr(), **opts)
+        reps = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            outs[name] = ctx.mult_device(sizes, offs, dsc.data_ptr(), **opts)
+        t = (time.perf_counter() - t0) / reps
+        res[name] = {"msm_per_s": m / t, "points_per_s": sum(sizes) / t, "ms_per_batch": 1e3 * t}
+        # e2e with host scalars
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            ctx.mult_uneven(sizes, offs, sc, **opts)
+        te = (time.perf_counter() - t0) / reps
+        res[name]["e2e_msm_per_s"] = m / te
+    res["ratio_batched_over_plain"] = res["batched"]["msm_per_s"] / res["plain"]["msm_per_s"]
+    res["e2e_ratio"] = res["batched"]["e2e_msm_per_s"] / res["plain"]["e2e_msm_per_s"]
+    res["identical_results"] = bool(np.array_equal(outs["plain"], outs["batched"]))
+    res["config"] = {"msms": m, "sizes": "log-uniform 2^10..2^20", "base_set": nbase,
+                     "scalars": "70% uniform, 10% 16-bit, 10% 0 or r-1, 10% repeated value"}
+    return res
+
+
+def bench_served(args, eng, ctx, n):
+    rng = np.random.default_rng(args.seed + 9)
+    nbase = min(n, 1 << 22)
+    m = args.served_requests
+    sizes = [int(2 ** u) for u in rng.uniform(12, 22, m)]
+    offs = [int(rng.integers(0, nbase - s + 1)) for s in sizes]
+    reqs = [eng.generate_scalars(args.seed + 100 + j, s) for j, s in enumerate(sizes)]
+    # plain: one request at a time
+    t0 = time.perf_counter()
+    plain_out = [ctx.mult_uneven([s], [o], r)[0] for s, o, r in zip(sizes, offs, reqs)]
+    t_plain = time.perf_counter() - t0
+    plain_rate = m / t_plain
+    out = {"plain_msm_per_s": plain_rate, "requests": m, "sizes": "log-uniform 2^12..2^22",
+           "base_set": nbase, "rates": []}
+    for mult in args.served_load:
+        lam = plain_rate * mult
+        gaps = rng.exponential(1.0 / lam, m)
+        srv = eng.MsmServer(ctx, hbm_budget_bytes=args.served_budget_gb << 30, max_inflight=2)
+        ids = []
+        t0 = time.perf_counter()
+        t_next = t0
+        for j in range(m):
+            t_next += gaps[j]
+            d = t_next - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            ids.append(srv.submit(reqs[j], offs[j]))
+        lats, exact = [], True
+        for j, rid in enumerate(ids):
+            o, l = srv.poll(rid, wait_ms=600000)
+            lats.append(l)
+            exact &= bool(np.array_equal(o, plain_out[j]))
+        t = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        out["rates"].append({"offered_per_s": lam, "msm_per_s": m / t, "p50_ms": percentile(lats, 50),
+                             "p99_ms": percentile(lats, 99), "passes": st["passes"],
+                             "inflight_peak": st["inflight_peak"], "same_as_alone": exact})
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--log2n", type=int, default=24)
+    ap.add_argument("--seed", type=int, default=20240601)
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-served", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-load", type=float, nargs="*", default=[0.5, 1.5])
+    ap.add_argument("--served-budget-gb", type=int, default=16)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        pass
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,278 @@
+// Base field of BLS12-377 (q, 377 bits) on sm_103a: twelve 32-bit limbs, Montgomery form with
+// R = 2^384 -- the same R as arkworks' six 64-bit limbs, so a device element is bit-for-bit the
+// arkworks Fq representation once it is fully reduced.
+//
+// Values are kept "lazy" in [0, 2q): 4q < 2^384, so the CIOS product of two such values is again
+// below 2q without a final subtraction.  Addition/subtraction reduce by 2q.  fq_canon() brings a
+// value to [0, q) for comparisons and for the ABI.
+//
+// The multiplier is operand-scanning CIOS on IMAD carry chains (mad.lo/madc.hi with .cc):
+// 4 x 12 multiply-adds plus one m = t0 * (-q^-1) per limb row, 588 IMAD per product.
+// The field is the one the reference computes in with GMP (host/msm_compute/include/
+// bls12_377_g1/bls12_377_g1.h:31-33, 90-219); the limb layout is new.
+#pragma once
+#include <stdint.h>
+
+#define FQ_LIMBS 12
+
+// q and 2q, little-endian 32-bit limbs
+#define BLS_Q {0x00000001u, 0x8508c000u, 0x30000000u, 0x170b5d44u, 0xba094800u, 0x1ef3622fu, 0x00f5138fu, 0x1a22d9f3u, 0x6ca1493bu, 0xc63b05c0u, 0x17c510eau, 0x01ae3a46u}
+#define BLS_Q2 {0x00000002u, 0x0a118000u, 0x60000001u, 0x2e16ba88u, 0x74129000u, 0x3de6c45fu, 0x01ea271eu, 0x3445b3e6u, 0xd9429276u, 0x8c760b80u, 0x2f8a21d5u, 0x035c748cu}
+// -q^-1 mod 2^32 (q = 1 mod 2^46)
+#define BLS_QINV 0xffffffffu
+// Montgomery-form constants (value * 2^384 mod q)
+#define BLS_ONE {0xffffff68u, 0x02cdffffu, 0x7fffffb1u, 0x51409f83u, 0x8a7d3ff2u, 0x9f7db3a9u, 0x6e7c6305u, 0x7b4e97b7u, 0x803c84e8u, 0x4cf495bfu, 0xe2fdf49au, 0x008d6661u}
+#define BLS_INV2 {0xffffffb4u, 0x8166ffffu, 0xbfffffd8u, 0x28a04fc1u, 0xc53e9ff9u, 0xcfbed9d4u, 0xb73e3182u, 0x3da74bdbu, 0xc01e4274u, 0x267a4adfu, 0xf17efa4du, 0x0046b330u}
+// twisted Edwards k = 2d and d (bls12_377_g1.h:37-39, 46-48)
+#define BLS_TE_K {0xbb58e892u, 0x33f6817bu, 0xff054e5du, 0x3fd664cau, 0xd6752edau, 0x6ad7181au, 0x47ff7cfeu, 0x55eabefau, 0x93fe9656u, 0xacf17111u, 0x199ed6ffu, 0x008d1a81u}
+#define BLS_TE_D {0xddac7449u, 0x99fb40bdu, 0x7f82a72eu, 0x1feb3265u, 0x6b3a976du, 0x356b8c0du, 0x23ffbe7fu, 0x2af55f7du, 0xc9ff4b2bu, 0xd678b888u, 0x8ccf6b7fu, 0x00468d40u}
+// Weierstrass -> Montgomery scale s (bls12_377_g1.h:40-42) and the twisted scale (:34-36)
+#define BLS_WS {0x27ce5f5fu, 0x171ef565u, 0x214ae372u, 0x6e5b6922u, 0x26a8cea6u, 0xc47c7b6au, 0x2d74b055u, 0xc22f509cu, 0xcbda4b0au, 0x0134cecbu, 0x229913d6u, 0x001ef3f3u}
+#define BLS_TWISTED_SCALE {0xe4aeaf1eu, 0x432a25c1u, 0xcd4c9661u, 0x5b39d21fu, 0xcd09455du, 0x692669ecu, 0x0f74f6bbu, 0xddae3345u, 0xabb65d37u, 0x76cbfeebu, 0x517df4cdu, 0x0143462fu}
+// 1/c_B and c_A/(3 c_B) of the Montgomery -> Weierstrass map (bls12_377_g1.h:366-374)
+#define BLS_INV_CB {0x776b1e1du, 0x455ce02fu, 0x63e0aa56u, 0x4b123b66u, 0x73fa6bf3u, 0x4d75723eu, 0x885e1101u, 0x468df1d4u, 0x638ee120u, 0x039e6c63u, 0x67cb3b82u, 0x005cdbd9u}
+#define BLS_CA_OVER_3CB {0x00000099u, 0x823ac000u, 0xb000004fu, 0xc5cabdc0u, 0x2f8c080du, 0x7f75ae86u, 0x9278b089u, 0x9ed4423bu, 0xec64c452u, 0x79467000u, 0x34c71c50u, 0x0120d3e4u}
+// q - 2, the Fermat inversion exponent
+#define BLS_QM2 {0xffffffffu, 0x8508bfffu, 0x30000000u, 0x170b5d44u, 0xba094800u, 0x1ef3622fu, 0x00f5138fu, 0x1a22d9f3u, 0x6ca1493bu, 0xc63b05c0u, 0x17c510eau, 0x01ae3a46u}
+
+struct fq_t {
+  uint32_t v[FQ_LIMBS];
+};
+
+// ---- carry-chain primitives (one PTX instruction each; the carry flag lives between them) ----
+__device__ __forceinline__ uint32_t madlo_cc(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t madclo_cc(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t madhi_cc(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t madchi_cc(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t madchi(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm volatile("madc.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
+}
+__device__ __forceinline__ uint32_t add_cc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t addc_cc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t addc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("addc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t sub_cc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t subc_cc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+__device__ __forceinline__ uint32_t subc(uint32_t a, uint32_t b) {
+  uint32_t r;
+  asm volatile("subc.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+  return r;
+}
+
+// ---- constructors ----
+__device__ __forceinline__ fq_t fq_from(const uint32_t (&c)[FQ_LIMBS]) {
+  fq_t r;
+#pragma unroll
+  for (int i = 0; i < FQ_LIMBS; i++) r.v[i] = c[i];
+  return r;
+}
+__device__ __forceinline__ fq_t fq_zero() {
+  fq_t r;
+#pragma unroll
+  for (int i = 0; i < FQ_LIMBS; i++) r.v[i] = 0;
+  return r;
+}
+__device__ __forceinline__ fq_t fq_one() {
+  const uint32_t c[FQ_LIMBS] = BLS_ONE;
+  return fq_from(c);
+}
+
+// ---- a * b * 2^-384 mod q (CIOS; inputs and output in [0, 2q)) ----
+__device__ __forceinline__ fq_t fq_mul(const fq_t &a, const fq_t &b) {
+  const uint32_t q[FQ_LIMBS] = BLS_Q;
+  uint32_t t[FQ_LIMBS + 1];
+#pragma unroll
+  for (int j = 0; j <= FQ_LIMBS; j++) t[j] = 0;
+#pragma unroll
+  for (int i = 0; i < FQ_LIMBS; i++) {
+    const uint32_t bi = b.v[i];
+    // t += a * b_i : low halves at j, high halves at j+1 (t[12] is 0 on entry)
+    t[0] = madlo_cc(a.v[0], bi, t[0]);
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS; j++) t[j] = madclo_cc(a.v[j], bi, t[j]);
+    t[FQ_LIMBS] = addc(0u, 0u);
+    t[1] = madhi_cc(a.v[0], bi, t[1]);
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS - 1; j++) t[j + 1] = madchi_cc(a.v[j], bi, t[j + 1]);
+    t[FQ_LIMBS] = madchi(a.v[FQ_LIMBS - 1], bi, t[FQ_LIMBS]);
+    // t += m * q with m chosen so that t[0] becomes 0
+    const uint32_t m = t[0] * BLS_QINV;
+    t[0] = madlo_cc(m, q[0], t[0]);
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS; j++) t[j] = madclo_cc(m, q[j], t[j]);
+    t[FQ_LIMBS] = addc(t[FQ_LIMBS], 0u);
+    t[1] = madhi_cc(m, q[0], t[1]);
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS - 1; j++) t[j + 1] = madchi_cc(m, q[j], t[j + 1]);
+    t[FQ_LIMBS] = madchi(m, q[FQ_LIMBS - 1], t[FQ_LIMBS]);
+    // divide by 2^32
+#pragma unroll
+    for (int j = 0; j < FQ_LIMBS; j++) t[j] = t[j + 1];
+    t[FQ_LIMBS] = 0;
+  }
+  fq_t r;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) r.v[j] = t[j];
+  return r;
+}
+
+__device__ __forceinline__ fq_t fq_sqr(const fq_t &a) { return fq_mul(a, a); }
+
+// r = x - 2q if x >= 2q else x   (x < 4q < 2^384)
+__device__ __forceinline__ fq_t fq_reduce_2q(const uint32_t (&x)[FQ_LIMBS]) {
+  const uint32_t q2[FQ_LIMBS] = BLS_Q2;
+  uint32_t d[FQ_LIMBS];
+  d[0] = sub_cc(x[0], q2[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) d[j] = subc_cc(x[j], q2[j]);
+  const uint32_t borrow = subc(0u, 0u);  // 0xffffffff if x < 2q
+  fq_t r;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) r.v[j] = borrow ? x[j] : d[j];
+  return r;
+}
+
+__device__ __forceinline__ fq_t fq_add(const fq_t &a, const fq_t &b) {
+  uint32_t s[FQ_LIMBS];
+  s[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) s[j] = addc_cc(a.v[j], b.v[j]);
+  s[FQ_LIMBS - 1] = addc(a.v[FQ_LIMBS - 1], b.v[FQ_LIMBS - 1]);
+  return fq_reduce_2q(s);
+}
+
+__device__ __forceinline__ fq_t fq_sub(const fq_t &a, const fq_t &b) {
+  const uint32_t q2[FQ_LIMBS] = BLS_Q2;
+  uint32_t d[FQ_LIMBS];
+  d[0] = sub_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) d[j] = subc_cc(a.v[j], b.v[j]);
+  const uint32_t mask = subc(0u, 0u);  // all ones on borrow
+  fq_t r;
+  r.v[0] = add_cc(d[0], q2[0] & mask);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) r.v[j] = addc_cc(d[j], q2[j] & mask);
+  r.v[FQ_LIMBS - 1] = addc(d[FQ_LIMBS - 1], q2[FQ_LIMBS - 1] & mask);
+  return r;
+}
+
+__device__ __forceinline__ fq_t fq_neg(const fq_t &a) { return fq_sub(fq_zero(), a); }
+
+__device__ __forceinline__ fq_t fq_dbl(const fq_t &a) { return fq_add(a, a); }
+
+// [0, 2q) -> [0, q)
+__device__ __forceinline__ fq_t fq_canon(const fq_t &a) {
+  const uint32_t q[FQ_LIMBS] = BLS_Q;
+  uint32_t d[FQ_LIMBS];
+  d[0] = sub_cc(a.v[0], q[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) d[j] = subc_cc(a.v[j], q[j]);
+  const uint32_t borrow = subc(0u, 0u);
+  fq_t r;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) r.v[j] = borrow ? a.v[j] : d[j];
+  return r;
+}
+
+__device__ __forceinline__ bool fq_is_zero(const fq_t &a) {
+  const fq_t c = fq_canon(a);
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) acc |= c.v[j];
+  return acc == 0;
+}
+
+__device__ __forceinline__ bool fq_eq(const fq_t &a, const fq_t &b) {
+  const fq_t x = fq_canon(a), y = fq_canon(b);
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) acc |= x.v[j] ^ y.v[j];
+  return acc == 0;
+}
+
+__device__ __forceinline__ fq_t fq_select(bool c, const fq_t &a, const fq_t &b) {
+  fq_t r;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) r.v[j] = c ? a.v[j] : b.v[j];
+  return r;
+}
+
+// a^(q-2) = a^-1 (0 -> 0): left-to-right 4-bit fixed windows over the exponent.
+static __device__ __noinline__ fq_t fq_inv(const fq_t &a) {
+  const uint32_t e[FQ_LIMBS] = BLS_QM2;
+  fq_t tbl[16];
+  tbl[0] = fq_one();
+  tbl[1] = a;
+#pragma unroll 1
+  for (int i = 2; i < 16; i++) tbl[i] = fq_mul(tbl[i - 1], a);
+  fq_t r = fq_one();
+  bool started = false;
+#pragma unroll 1
+  for (int w = FQ_LIMBS * 8 - 1; w >= 0; w--) {
+    const uint32_t nib = (e[w >> 3] >> ((w & 7) * 4)) & 15u;
+    if (started) {
+      r = fq_sqr(r);
+      r = fq_sqr(r);
+      r = fq_sqr(r);
+      r = fq_sqr(r);
+    }
+    if (nib) {
+      r = started ? fq_mul(r, tbl[nib]) : tbl[nib];
+      started = true;
+    }
+  }
+  return r;
+}
+
+// ---- 16-byte vector loads/stores of field elements ----
+__device__ __forceinline__ void fq_load(fq_t &r, const uint4 *p) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const uint4 u = p[k];
+    r.v[4 * k + 0] = u.x;
+    r.v[4 * k + 1] = u.y;
+    r.v[4 * k + 2] = u.z;
+    r.v[4 * k + 3] = u.w;
+  }
+}
+__device__ __forceinline__ void fq_store(uint4 *p, const fq_t &a) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) p[k] = make_uint4(a.v[4 * k], a.v[4 * k + 1], a.v[4 * k + 2], a.v[4 * k + 3]);
+}

@@ -1,0 +1,1318 @@
+// Host side of libdriver.so: the C ABI of include/msm_gb300.h over the device pipeline.
+//
+// It mirrors the reference host driver (zprize/msm_pippenger/host/driver/driver.cpp):
+//   msm_init  -> Driver::Driver + load_xclbin (driver.cpp:137-304): bases converted once to the
+//                precomputed twisted-Edwards form, here on the GPU, and kept resident in HBM;
+//                bases without a twisted-Edwards image are listed for the Weierstrass path
+//                (driver.cpp:158-171);
+//   msm_mult  -> run_asynchronous (driver.cpp:495-600): scalars of batch b+1 cross PCIe/C2C while
+//                batch b computes; everything after the scalars (sort, buckets, reduction,
+//                window combine, affine map) runs on the device and only 144 B per MSM return.
+// Additions: uneven batches in one pass with one shared sort, CUDA-graph replay, an autotuner,
+// a continuous-batching server, per-stage timing and data generators for tests and benchmarks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/msm_gb300.h"
+#include "engine.h"
+
+static_assert(sizeof(biginteger256_t) == 32, "biginteger256_t is 32 bytes");
+static_assert(sizeof(g1_affine_t) == 104, "g1_affine_t is 104 bytes");
+static_assert(offsetof(g1_affine_t, infinity) == 96, "g1_affine_t.infinity at byte 96");
+static_assert(sizeof(g1_projective_t) == 144, "g1_projective_t is 144 bytes");
+
+// ---------------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+thread_local int g_err = 0;
+thread_local char g_msg[512] = {0};
+
+enum {
+  ERR_ARG = -1,
+  ERR_CUDA = -2,
+  ERR_INPUT = -3,
+  ERR_DEVICE = -4,
+  ERR_BUDGET = -5,
+  ERR_STATE = -6,
+};
+
+int fail(int code, const char *fmt, ...) {
+  g_err = code;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),   \
+                  __FILE__, __LINE__);                                                \
+  } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // grow-only; returns true if the address changed
+  cudaError_t ensure(size_t want, bool *moved = nullptr) {
+    if (want <= bytes && p) return cudaSuccess;
+    release();
+    size_t sz = std::max<size_t>(want, 256);
+    cudaError_t e = cudaMalloc(&p, sz);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    bytes = sz;
+    if (moved) *moved = true;
+    return cudaSuccess;
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+struct HostPinned {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(want, 256));
+    if (e == cudaSuccess) bytes = std::max<size_t>(want, 256);
+    return e;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// configuration
+// ---------------------------------------------------------------------------------------------
+struct Cfg {
+  uint32_t c = 16;
+  uint32_t signed_digits = 1;
+  uint32_t seg_len = 1024;
+  uint32_t red_log2 = 5;
+};
+
+uint32_t windows_of(uint32_t c) { return (MSM_SCALAR_BITS + c - 1) / c; }
+
+uint32_t log2_ceil(uint64_t n) {
+  uint32_t k = 0;
+  while ((1ull << k) < n) k++;
+  return k;
+}
+
+// bucket counts of a window layout (signed: 2^(c-1) per window, the top one 2^c_top; unsigned:
+// 2^c - 1 and 2^c_top - 1)
+void layout(uint32_t c, uint32_t sgn, uint32_t &nwin, uint32_t &nb, uint32_t &nb_top) {
+  nwin = windows_of(c);
+  const uint32_t ctop = MSM_SCALAR_BITS - c * (nwin - 1);
+  if (sgn) {
+    nb = 1u << (c - 1);
+    nb_top = 1u << ctop;
+  } else {
+    nb = (1u << c) - 1;
+    nb_top = (1u << ctop) - 1;
+  }
+}
+
+// cost model in 12-limb multiplications: 7 per bucket add, 18 per bucket in the reduction
+double model_cost(uint64_t n, uint32_t c, uint32_t sgn) {
+  uint32_t nwin, nb, nbt;
+  layout(c, sgn, nwin, nb, nbt);
+  const double buckets = (double)(nwin - 1) * nb + nbt;
+  return (double)n * nwin * 7.0 + buckets * 18.0 + (double)nwin * 4000.0;
+}
+
+Cfg heuristic_cfg(uint64_t n) {
+  Cfg cfg;
+  double best = 1e300;
+  for (uint32_t c = 6; c <= 20; c++) {
+    const double v = model_cost(n, c, 1);
+    if (v < best) {
+      best = v;
+      cfg.c = c;
+    }
+  }
+  uint32_t nwin, nb, nbt;
+  layout(cfg.c, 1, nwin, nb, nbt);
+  const double mean = (double)n / nb;  // entries per bucket per window
+  uint32_t s = 32;
+  while (s < 2 * mean && s < 4096) s <<= 1;
+  cfg.seg_len = s;
+  // level-1 segment length L with 2L ~ 3 nb / (128 L) adds per thread on both levels
+  const double l = std::sqrt(3.0 * nb / 256.0);
+  cfg.red_log2 = std::min<uint32_t>(std::max<uint32_t>(log2_ceil((uint64_t)std::max(1.0, l)), 2), 10);
+  return cfg;
+}
+
+// ---------------------------------------------------------------------------------------------
+// pass plan
+// ---------------------------------------------------------------------------------------------
+struct JobSpec {
+  uint64_t n, base_off, scalar_off;
+  Cfg cfg;
+};
+
+struct Plan {
+  std::vector<JobDesc> jobs;
+  std::vector<WinDesc> wins;
+  uint64_t n_points = 0, max_entries = 0;
+  uint32_t n_buckets = 0, n_segs = 0, max_tasks = 0;
+  uint32_t seg_len = 1024, red_log2 = 5;
+  std::string key;
+};
+
+int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
+  pl = Plan();
+  if (specs.empty()) return fail(ERR_ARG, "empty pass");
+  pl.seg_len = specs[0].cfg.seg_len;
+  pl.red_log2 = specs[0].cfg.red_log2;
+  uint64_t buckets = 0, segs = 0, wins = 0;
+  char tmp[160];
+  for (size_t j = 0; j < specs.size(); j++) {
+    const JobSpec &s = specs[j];
+    JobDesc d{};
+    d.point_begin = pl.n_points;
+    d.n = s.n;
+    d.base_off = s.base_off;
+    d.scalar_off = s.scalar_off;
+    d.c = s.cfg.c;
+    d.signed_digits = s.cfg.signed_digits;
+    d.result_slot = (uint32_t)j;
+    d.bucket_begin = (uint32_t)buckets;
+    d.win_begin = (uint32_t)wins;
+    if (s.n == 0) {
+      d.nwin = 0;
+      d.nb = d.nb_top = 0;
+    } else {
+      layout(d.c, d.signed_digits, d.nwin, d.nb, d.nb_top);
+      const uint32_t L = 1u << pl.red_log2;
+      for (uint32_t w = 0; w < d.nwin; w++) {
+        WinDesc wd{};
+        wd.job = (uint32_t)j;
+        wd.w = w;
+        wd.bucket_begin = (uint32_t)(buckets + (uint64_t)w * d.nb);
+        wd.nb = (w + 1 == d.nwin) ? d.nb_top : d.nb;
+        wd.seg_begin = (uint32_t)segs;
+        wd.nseg = (wd.nb + L - 1) / L;
+        segs += wd.nseg;
+        pl.wins.push_back(wd);
+      }
+      buckets += (uint64_t)(d.nwin - 1) * d.nb + d.nb_top;
+      wins += d.nwin;
+      pl.max_entries += s.n * d.nwin;
+    }
+    pl.n_points += s.n;
+    pl.jobs.push_back(d);
+    snprintf(tmp, sizeof(tmp), "%llu/%llu/%llu/%u/%u;", (unsigned long long)s.n,
+             (unsigned long long)s.base_off, (unsigned long long)s.scalar_off, d.c, d.signed_digits);
+    pl.key += tmp;
+  }
+  if (buckets >= (1ull << 32) || pl.max_entries >= (1ull << 32) - 1 || segs >= (1ull << 31))
+    return fail(ERR_BUDGET, "pass too large: %llu buckets, %llu entries",
+                (unsigned long long)buckets, (unsigned long long)pl.max_entries);
+  pl.n_buckets = (uint32_t)buckets;
+  pl.n_segs = (uint32_t)segs;
+  const uint64_t mt = buckets + pl.max_entries / pl.seg_len + 1;
+  if (mt >= (1ull << 31)) return fail(ERR_BUDGET, "too many tasks");
+  pl.max_tasks = (uint32_t)mt;
+  snprintf(tmp, sizeof(tmp), "|%u|%u", pl.seg_len, pl.red_log2);
+  pl.key += tmp;
+  return 0;
+}
+
+// device bytes a pass needs besides the resident bases
+uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
+  uint64_t b = 0;
+  b += (uint64_t)pl.n_buckets * 4 * 5;                   // count, offset, fill, taskoff, heavy
+  b += pl.max_entries * 4;                                // vals
+  b += (uint64_t)pl.max_tasks * (sizeof(Task) + MSM_BUCKET_BYTES);
+  b += (uint64_t)pl.n_segs * 2 * MSM_BUCKET_BYTES;
+  b += (uint64_t)pl.wins.size() * MSM_BUCKET_BYTES;
+  b += pl.jobs.size() * (sizeof(JobDesc) + MSM_PROJ_BYTES) + pl.wins.size() * sizeof(WinDesc);
+  if (with_scalars) b += pl.n_points * 32;
+  return b + (1 << 20);
+}
+
+// ---------------------------------------------------------------------------------------------
+// workspace: the buffers of one in-flight pass
+// ---------------------------------------------------------------------------------------------
+struct Workspace {
+  DevBuf count, offset, fill, taskoff, scan_tmp, vals, tasks, partials, heavy, counters, seg_out,
+      win_sum, results, jobs, wins;
+  DevBuf scalars[2];
+  HostPinned res_host;
+  cudaEvent_t ev[10] = {};
+  uint64_t generation = 0;  // bumps when any buffer moves (graphs must be re-captured)
+  std::unordered_map<std::string, cudaGraphExec_t> graphs;
+
+  ~Workspace() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  int ensure(const Plan &pl) {
+    bool moved = false;
+    CK(count.ensure((size_t)pl.n_buckets * 4, &moved));
+    CK(offset.ensure((size_t)pl.n_buckets * 4, &moved));
+    CK(fill.ensure((size_t)pl.n_buckets * 4, &moved));
+    CK(taskoff.ensure((size_t)pl.n_buckets * 4, &moved));
+    CK(heavy.ensure((size_t)pl.n_buckets * 4, &moved));
+    CK(scan_tmp.ensure(msm_scan_tmp_words(pl.n_buckets) * 4, &moved));
+    CK(vals.ensure((size_t)pl.max_entries * 4, &moved));
+    CK(tasks.ensure((size_t)pl.max_tasks * sizeof(Task), &moved));
+    CK(partials.ensure((size_t)pl.max_tasks * MSM_BUCKET_BYTES, &moved));
+    CK(counters.ensure(CNT_WORDS * 4, &moved));
+    CK(seg_out.ensure((size_t)pl.n_segs * 2 * MSM_BUCKET_BYTES, &moved));
+    CK(win_sum.ensure(pl.wins.size() * MSM_BUCKET_BYTES, &moved));
+    CK(results.ensure(pl.jobs.size() * MSM_PROJ_BYTES, &moved));
+    CK(jobs.ensure(pl.jobs.size() * sizeof(JobDesc), &moved));
+    CK(wins.ensure(pl.wins.size() * sizeof(WinDesc), &moved));
+    CK(res_host.ensure(pl.jobs.size() * MSM_PROJ_BYTES));
+    if (!ev[0])
+      for (auto &e : ev) CK(cudaEventCreate(&e));
+    if (moved) {
+      generation++;
+      for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+      graphs.clear();
+    }
+    return 0;
+  }
+  [[maybe_unused]] void release_sort_buffers() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
+    scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
+    win_sum.release(); scalars[0].release(); scalars[1].release();
+    generation++;
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------------
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  uint64_t npoints = 0;
+  DevBuf bases, flags, special_idx, special_cls, class_pts;
+  uint32_t n_special = 0, n_classes = 0;
+  cudaStream_t stream = nullptr, copy_stream = nullptr;
+  cudaEvent_t copied[2] = {}, freed[2] = {};
+  Workspace ws;
+  std::mutex mu;
+  bool timing = false;
+  double last_ms[MSM_NUM_STAGES] = {0};
+  uint64_t last_stats[4] = {0};
+  std::map<uint32_t, Cfg> tuned;  // by log2 size class
+  ~Ctx() {
+    if (stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    for (int i = 0; i < 2; i++) {
+      if (copied[i]) cudaEventDestroy(copied[i]);
+      if (freed[i]) cudaEventDestroy(freed[i]);
+    }
+  }
+};
+
+PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars) {
+  PassBuffers pb{};
+  pb.bases = cx->bases.as<uint4>();
+  pb.flags = cx->flags.as<uint8_t>();
+  pb.special_idx = cx->special_idx.as<uint32_t>();
+  pb.special_cls = cx->special_cls.as<uint8_t>();
+  pb.class_pts = cx->class_pts.as<uint4>();
+  pb.n_special = cx->n_special;
+  pb.n_classes = cx->n_classes;
+  pb.n_bases = cx->npoints;
+  pb.scalars = (const uint4 *)d_scalars;
+  pb.jobs = ws.jobs.as<JobDesc>();
+  pb.wins = ws.wins.as<WinDesc>();
+  pb.n_jobs = (uint32_t)pl.jobs.size();
+  pb.n_wins = (uint32_t)pl.wins.size();
+  pb.n_points = pl.n_points;
+  pb.n_buckets = pl.n_buckets;
+  pb.n_segs = pl.n_segs;
+  pb.seg_len = pl.seg_len;
+  pb.red_len_log2 = pl.red_log2;
+  pb.max_entries = pl.max_entries;
+  pb.max_tasks = pl.max_tasks;
+  pb.count = ws.count.as<uint32_t>();
+  pb.offset = ws.offset.as<uint32_t>();
+  pb.fill = ws.fill.as<uint32_t>();
+  pb.taskoff = ws.taskoff.as<uint32_t>();
+  pb.scan_tmp = ws.scan_tmp.as<uint32_t>();
+  pb.vals = ws.vals.as<uint32_t>();
+  pb.tasks = ws.tasks.as<Task>();
+  pb.partials = ws.partials.as<uint4>();
+  pb.heavy = ws.heavy.as<uint32_t>();
+  pb.counters = ws.counters.as<uint32_t>();
+  pb.seg_out = ws.seg_out.as<uint4>();
+  pb.win_sum = ws.win_sum.as<uint4>();
+  pb.results = ws.results.as<uint64_t>();
+  return pb;
+}
+
+// Enqueue one pass on `st`: upload the plan, run the pipeline (directly or from a captured
+// graph), copy the results to ws.res_host + res_offset jobs.  Does not synchronize.
+int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, cudaStream_t st,
+                 bool use_graph, bool timing, size_t res_offset) {
+  if (ws.ensure(pl)) return g_err;
+  CK(cudaMemcpyAsync(ws.jobs.p, pl.jobs.data(), pl.jobs.size() * sizeof(JobDesc),
+                     cudaMemcpyHostToDevice, st));
+  if (!pl.wins.empty())
+    CK(cudaMemcpyAsync(ws.wins.p, pl.wins.data(), pl.wins.size() * sizeof(WinDesc),
+                       cudaMemcpyHostToDevice, st));
+  const PassBuffers pb = make_pass_buffers(cx, ws, pl, d_scalars);
+  char *res_dst = (char *)ws.res_host.p;
+  if (res_offset * MSM_PROJ_BYTES + pl.jobs.size() * MSM_PROJ_BYTES > ws.res_host.bytes)
+    return fail(ERR_STATE, "result staging too small");
+  res_dst += res_offset * MSM_PROJ_BYTES;
+  if (use_graph && !timing) {
+    char tmp[64];
+    snprintf(tmp, sizeof(tmp), "#%p#%p", d_scalars, (void *)res_dst);
+    const std::string key = pl.key + tmp;
+    auto it = ws.graphs.find(key);
+    if (it == ws.graphs.end()) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = msm_launch_pass(pb, cx->num_sms, st, nullptr);
+      cudaError_t e2 = cudaMemcpyAsync(res_dst, ws.results.p, pl.jobs.size() * MSM_PROJ_BYTES,
+                                       cudaMemcpyDeviceToHost, st);
+      cudaError_t e3 = cudaStreamEndCapture(st, &g);
+      if (e != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+        return fail(ERR_CUDA, "graph capture failed: %s / %s / %s", cudaGetErrorString(e),
+                    cudaGetErrorString(e2), cudaGetErrorString(e3));
+      cudaGraphExec_t ex;
+      CK(cudaGraphInstantiate(&ex, g, 0));
+      cudaGraphDestroy(g);
+      it = ws.graphs.emplace(key, ex).first;
+    }
+    CK(cudaGraphLaunch(it->second, st));
+    return 0;
+  }
+  CK(msm_launch_pass(pb, cx->num_sms, st, timing ? ws.ev : nullptr));
+  CK(cudaMemcpyAsync(res_dst, ws.results.p, pl.jobs.size() * MSM_PROJ_BYTES,
+                     cudaMemcpyDeviceToHost, st));
+  return 0;
+}
+
+int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
+  uint32_t cnt[CNT_WORDS];
+  CK(cudaMemcpyAsync(cnt, ws.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (stats_out) {
+    stats_out[0] = cnt[CNT_TASKS];
+    stats_out[1] = cnt[CNT_HEAVY];
+  }
+  if (cnt[CNT_ERROR])
+    return fail(ERR_STATE, "device bounds check %u fired (info %u)", cnt[CNT_ERROR],
+                cnt[CNT_ERROR_INFO]);
+  return 0;
+}
+
+Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
+  Cfg cfg = heuristic_cfg(n);
+  auto it = cx->tuned.find(log2_ceil(std::max<uint64_t>(n, 1)));
+  if (it != cx->tuned.end()) cfg = it->second;
+  if (opt) {
+    if (opt->window_bits > 0) {
+      cfg.c = (uint32_t)std::min(std::max(opt->window_bits, 4), 22);
+      uint32_t nwin, nb, nbt;
+      layout(cfg.c, 1, nwin, nb, nbt);
+      const double mean = (double)n / nb;
+      uint32_t s = 32;
+      while (s < 2 * mean && s < 4096) s <<= 1;
+      cfg.seg_len = s;
+      const double l = std::sqrt(3.0 * nb / 256.0);
+      cfg.red_log2 =
+          std::min<uint32_t>(std::max<uint32_t>(log2_ceil((uint64_t)std::max(1.0, l)), 2), 10);
+    }
+    if (opt->signed_digits == 1) cfg.signed_digits = 1;
+    if (opt->signed_digits == 2) cfg.signed_digits = 0;
+    if (opt->seg_len > 0) cfg.seg_len = (uint32_t)opt->seg_len;
+    if (opt->red_len_log2 > 0) cfg.red_log2 = (uint32_t)std::min(opt->red_len_log2, 12);
+  }
+  if (!cfg.signed_digits && cfg.c > 21) cfg.c = 21;
+  return cfg;
+}
+
+void record_timings(Ctx *cx, Workspace &ws) {
+  for (int k = 0; k < MSM_NUM_STAGES; k++) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ws.ev[k], ws.ev[k + 1]) != cudaSuccess) ms = -1;
+    cx->last_ms[k] = ms;
+  }
+}
+
+// Run a list of MSMs whose scalars are in host memory (d_scalars == nullptr) or already on the
+// device.  mode 1: one pass per MSM with the next MSM's scalars copied during the current pass;
+// mode 2: all MSMs in one pass with one shared sort.
+int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
+             const std::vector<uint64_t> &offs, const biginteger256_t *h_scalars,
+             const void *d_scalars, const msm_options_t *opt) {
+  const size_t m = sizes.size();
+  if (m == 0) return 0;
+  for (size_t j = 0; j < m; j++)
+    if (offs[j] > cx->npoints || sizes[j] > cx->npoints - offs[j])
+      return fail(ERR_ARG, "MSM %zu: bases [%llu, %llu) outside the %llu resident bases", j,
+                  (unsigned long long)offs[j], (unsigned long long)(offs[j] + sizes[j]),
+                  (unsigned long long)cx->npoints);
+  const int mode = (opt && opt->mode == 2) ? 2 : 1;
+  const bool use_graph = !(opt && opt->use_graph == 2) && !cx->timing;
+  Workspace &ws = cx->ws;
+  std::vector<uint64_t> first(m + 1, 0);
+  for (size_t j = 0; j < m; j++) first[j + 1] = first[j] + sizes[j];
+
+  if (mode == 2) {
+    std::vector<JobSpec> specs(m);
+    uint64_t maxn = 0;
+    for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
+    for (size_t j = 0; j < m; j++) {
+      specs[j] = {sizes[j], offs[j], first[j], resolve_cfg(cx, sizes[j], opt)};
+      specs[j].cfg.seg_len = resolve_cfg(cx, maxn, opt).seg_len;
+      specs[j].cfg.red_log2 = resolve_cfg(cx, maxn, opt).red_log2;
+    }
+    Plan pl;
+    if (build_plan(specs, pl)) return g_err;
+    const void *src = d_scalars;
+    if (!src) {
+      CK(ws.scalars[0].ensure(first[m] * 32));
+      if (first[m]) CK(cudaMemcpyAsync(ws.scalars[0].p, h_scalars, first[m] * 32,
+                                       cudaMemcpyHostToDevice, cx->stream));
+      src = ws.scalars[0].p;
+    }
+    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, 0)) return g_err;
+    if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
+    if (cx->timing) record_timings(cx, ws);
+    cx->last_stats[2] = pl.max_entries;
+    cx->last_stats[3] = pl.n_buckets;
+    memcpy(out, ws.res_host.p, m * MSM_PROJ_BYTES);
+    return 0;
+  }
+
+  // mode 1: one pass per MSM; results land in ws.res_host at slot j
+  Plan probe;
+  {
+    std::vector<JobSpec> one(1);
+    uint64_t maxn = 0;
+    for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
+    one[0] = {maxn, 0, 0, resolve_cfg(cx, maxn, opt)};
+    if (build_plan(one, probe)) return g_err;
+    if (ws.ensure(probe)) return g_err;
+  }
+  CK(ws.res_host.ensure(m * MSM_PROJ_BYTES));
+  uint64_t maxn = 0;
+  for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
+  if (!d_scalars)
+    for (int s = 0; s < 2; s++) CK(ws.scalars[s].ensure(std::max<uint64_t>(maxn, 1) * 32));
+  for (size_t j = 0; j < m; j++) {
+    std::vector<JobSpec> one(1);
+    one[0] = {sizes[j], offs[j], d_scalars ? first[j] : 0, resolve_cfg(cx, sizes[j], opt)};
+    Plan pl;
+    if (build_plan(one, pl)) return g_err;
+    const void *src = d_scalars;
+    if (!src) {
+      const int slot = (int)(j & 1);
+      CK(cudaStreamWaitEvent(cx->copy_stream, cx->freed[slot], 0));
+      if (sizes[j])
+        CK(cudaMemcpyAsync(ws.scalars[slot].p, h_scalars + first[j], sizes[j] * 32,
+                           cudaMemcpyHostToDevice, cx->copy_stream));
+      CK(cudaEventRecord(cx->copied[slot], cx->copy_stream));
+      CK(cudaStreamWaitEvent(cx->stream, cx->copied[slot], 0));
+      src = ws.scalars[slot].p;
+    }
+    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, j)) return g_err;
+    if (!d_scalars) CK(cudaEventRecord(cx->freed[(int)(j & 1)], cx->stream));
+    if (cx->timing) {
+      if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
+      record_timings(cx, ws);
+      cx->last_stats[2] = pl.max_entries;
+      cx->last_stats[3] = pl.n_buckets;
+    }
+  }
+  if (check_pass_errors(ws, cx->stream, cx->timing ? nullptr : cx->last_stats)) return g_err;
+  memcpy(out, ws.res_host.p, m * MSM_PROJ_BYTES);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// init: resident bases
+// ---------------------------------------------------------------------------------------------
+int init_device(Ctx *cx) {
+  const char *dev = getenv("MSM_DEVICE");
+  cx->device = dev ? atoi(dev) : 0;
+  CK(cudaSetDevice(cx->device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, cx->device));
+  cx->num_sms = prop.multiProcessorCount;
+  CK(cudaStreamCreateWithFlags(&cx->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&cx->copy_stream, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; i++) {
+    CK(cudaEventCreateWithFlags(&cx->copied[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&cx->freed[i], cudaEventDisableTiming));
+    CK(cudaEventRecord(cx->freed[i], cx->stream));
+  }
+  return 0;
+}
+
+int load_bases(Ctx *cx, const g1_affine_t *points, uint64_t n) {
+  cx->npoints = n;
+  CK(cx->bases.ensure(std::max<uint64_t>(n, 1) * MSM_BASE_BYTES));
+  CK(cx->flags.ensure(std::max<uint64_t>(n, 1)));
+  CK(cx->special_idx.ensure(std::max<uint64_t>(n, 1) * 4));
+  DevBuf cnt, staging;
+  CK(cnt.ensure(4));
+  CK(cudaMemsetAsync(cnt.p, 0, 4, cx->stream));
+  const uint64_t chunk = std::min<uint64_t>(std::max<uint64_t>(n, 1), 1ull << 22);
+  CK(staging.ensure(chunk * MSM_AFFINE_BYTES));
+  for (uint64_t i0 = 0; i0 < n; i0 += chunk) {
+    const uint64_t k = std::min(chunk, n - i0);
+    CK(cudaMemcpyAsync(staging.p, points + i0, k * MSM_AFFINE_BYTES, cudaMemcpyHostToDevice,
+                       cx->stream));
+    CK(msm_launch_precompute(staging.p, k, cx->bases.as<uint4>() + i0 * 9,
+                             cx->flags.as<uint8_t>() + i0, cx->special_idx.as<uint32_t>(),
+                             cnt.as<uint32_t>(), (uint32_t)i0, cx->stream));
+  }
+  uint32_t nspecial = 0;
+  CK(cudaMemcpyAsync(&nspecial, cnt.p, 4, cudaMemcpyDeviceToHost, cx->stream));
+  CK(cudaStreamSynchronize(cx->stream));
+  // reject coordinates that are not reduced field elements
+  {
+    std::vector<uint8_t> fl(n);
+    CK(cudaMemcpy(fl.data(), cx->flags.p, n, cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < n; i++)
+      if (fl[i] == BASE_BAD_INPUT)
+        return fail(ERR_INPUT, "point %llu: coordinate not below the field modulus",
+                    (unsigned long long)i);
+  }
+  cx->n_special = nspecial;
+  cx->n_classes = 0;
+  if (nspecial) {
+    // group the special bases into classes of equal points (at most 5 exist on the curve:
+    // three of order 2 with y = 0 and two of order 4 with Montgomery u = -1)
+    std::vector<uint32_t> idx(nspecial);
+    CK(cudaMemcpy(idx.data(), cx->special_idx.p, nspecial * 4, cudaMemcpyDeviceToHost));
+    std::sort(idx.begin(), idx.end());
+    CK(cudaMemcpy(cx->special_idx.p, idx.data(), nspecial * 4, cudaMemcpyHostToDevice));
+    std::vector<uint8_t> cls(nspecial);
+    std::vector<uint32_t> class_words;  // 24 u32 per class: x then y
+    for (uint32_t s = 0; s < nspecial; s++) {
+      const g1_affine_t &p = points[idx[s]];
+      int found = -1;
+      for (uint32_t c = 0; c < cx->n_classes; c++)
+        if (!memcmp(&class_words[c * 24], p.x.data, 48) &&
+            !memcmp(&class_words[c * 24 + 12], p.y.data, 48))
+          found = (int)c;
+      if (found < 0) {
+        if (cx->n_classes == 8)
+          return fail(ERR_INPUT, "more than 8 distinct points without a twisted-Edwards image");
+        class_words.resize((cx->n_classes + 1) * 24);
+        memcpy(&class_words[cx->n_classes * 24], p.x.data, 48);
+        memcpy(&class_words[cx->n_classes * 24 + 12], p.y.data, 48);
+        found = (int)cx->n_classes++;
+      }
+      cls[s] = (uint8_t)found;
+    }
+    CK(cx->special_cls.ensure(nspecial));
+    CK(cudaMemcpy(cx->special_cls.p, cls.data(), nspecial, cudaMemcpyHostToDevice));
+    CK(cx->class_pts.ensure(cx->n_classes * 96));
+    CK(cudaMemcpy(cx->class_pts.p, class_words.data(), cx->n_classes * 96, cudaMemcpyHostToDevice));
+    DevBuf ok;
+    CK(ok.ensure(cx->n_classes * 4));
+    CK(msm_launch_check_classes(cx->class_pts.as<uint4>(), cx->n_classes, ok.as<uint32_t>(),
+                                cx->stream));
+    std::vector<uint32_t> okh(cx->n_classes);
+    CK(cudaMemcpyAsync(okh.data(), ok.p, cx->n_classes * 4, cudaMemcpyDeviceToHost, cx->stream));
+    CK(cudaStreamSynchronize(cx->stream));
+    for (uint32_t c = 0; c < cx->n_classes; c++)
+      if (!okh[c])
+        return fail(ERR_INPUT, "a point without a twisted-Edwards image is not a curve point of "
+                               "order 2 or 4");
+  } else {
+    CK(cx->special_cls.ensure(1));
+    CK(cx->class_pts.ensure(96));
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// host generators (SplitMix64, counter-based; the same function as the oracle's and the GPU's)
+// ---------------------------------------------------------------------------------------------
+inline uint64_t splitmix64(uint64_t x) {
+  uint64_t z = x + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+inline uint64_t rand_u64(uint64_t seed, uint64_t stream, uint64_t index, uint64_t word) {
+  const uint64_t s = splitmix64(seed ^ (stream * 0xD1B54A32D192ED03ull));
+  const uint64_t h = splitmix64(s ^ splitmix64(index));
+  return splitmix64(h + word);
+}
+const uint64_t R_WORDS[4] = {0x0a11800000000001ull, 0x59aa76fed0000001ull, 0x60b44d1e5c37b001ull,
+                             0x12ab655e9a2ca556ull};
+inline bool lt_r(const uint64_t *v) {
+  for (int k = 3; k >= 0; k--) {
+    if (v[k] < R_WORDS[k]) return true;
+    if (v[k] > R_WORDS[k]) return false;
+  }
+  return false;
+}
+void uniform_scalar(uint64_t seed, uint64_t i, uint64_t *out, uint64_t stream = 2) {
+  for (uint64_t a = 0;; a++) {
+    for (int j = 0; j < 4; j++) out[j] = rand_u64(seed, stream, i, 4 * a + j);
+    out[3] &= (1ull << 61) - 1;
+    if (lt_r(out)) return;
+  }
+}
+void mixed_scalar(uint64_t seed, uint64_t msm, uint64_t i, uint64_t *out) {
+  const uint64_t key = (msm << 32) | i;
+  const uint64_t sel = rand_u64(seed, 3, key, 0) % 10;
+  if (sel < 7) return uniform_scalar(seed, key, out);
+  if (sel == 7) {
+    out[0] = rand_u64(seed, 3, key, 1) & 0xffff;
+    out[1] = out[2] = out[3] = 0;
+    return;
+  }
+  if (sel == 8) {
+    if ((rand_u64(seed, 3, key, 2) & 1) == 0) {
+      out[0] = out[1] = out[2] = out[3] = 0;
+    } else {
+      for (int k = 0; k < 4; k++) out[k] = R_WORDS[k];
+      out[0] -= 1;
+    }
+    return;
+  }
+  uniform_scalar(seed, (msm << 32) | 0xffffffffull, out);
+}
+
+// ---------------------------------------------------------------------------------------------
+// server: continuous batching
+// ---------------------------------------------------------------------------------------------
+struct Request {
+  int64_t id;
+  uint64_t n, base_off;
+  std::vector<biginteger256_t> scalars;
+  uint8_t result[MSM_PROJ_BYTES];
+  int status = 1;  // 1 pending/running, 0 done, <0 error
+  std::chrono::steady_clock::time_point t_submit, t_done;
+};
+
+struct Slot {
+  Workspace ws;
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  bool busy = false;
+  uint64_t bytes = 0;
+  std::vector<std::shared_ptr<Request>> reqs;
+  DevBuf scal;
+  Plan plan;
+};
+
+struct Server {
+  Ctx *cx = nullptr;
+  uint64_t budget = 0;
+  int max_inflight = 2;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::mutex mu;
+  std::condition_variable cv, cv_done;
+  std::deque<std::shared_ptr<Request>> pending;
+  std::unordered_map<int64_t, std::shared_ptr<Request>> all;
+  std::atomic<bool> stop{false};
+  std::thread worker;
+  int64_t next_id = 0;
+  uint64_t bytes_in_use = 0;
+  msm_server_stats_t stats{};
+
+  uint64_t request_bytes(uint64_t n) {
+    std::vector<JobSpec> one(1);
+    one[0] = {n, 0, 0, resolve_cfg(cx, n, nullptr)};
+    Plan pl;
+    if (build_plan(one, pl)) return ~0ull;
+    return plan_bytes(pl, true);
+  }
+
+  void loop();
+};
+
+void Server::loop() {
+  std::unique_lock<std::mutex> lk(mu);
+  while (!stop) {
+    // retire finished passes
+    bool any_done = false;
+    for (auto &sl : slots) {
+      if (!sl->busy) continue;
+      if (cudaEventQuery(sl->done) == cudaSuccess) {
+        uint32_t cnt[CNT_WORDS];
+        cudaMemcpy(cnt, sl->ws.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost);
+        const auto now = std::chrono::steady_clock::now();
+        for (size_t j = 0; j < sl->reqs.size(); j++) {
+          auto &r = sl->reqs[j];
+          memcpy(r->result, (char *)sl->ws.res_host.p + j * MSM_PROJ_BYTES, MSM_PROJ_BYTES);
+          r->status = cnt[CNT_ERROR] ? ERR_STATE : 0;
+          r->t_done = now;
+          stats.completed++;
+        }
+        sl->reqs.clear();
+        bytes_in_use -= sl->bytes;
+        sl->bytes = 0;
+        sl->busy = false;
+        any_done = true;
+      }
+    }
+    if (any_done) cv_done.notify_all();
+    // admit: every pending request that fits the budget joins one pass on a free slot
+    Slot *free_slot = nullptr;
+    for (auto &sl : slots)
+      if (!sl->busy) {
+        free_slot = sl.get();
+        break;
+      }
+    if (free_slot && !pending.empty()) {
+      std::vector<std::shared_ptr<Request>> batch;
+      uint64_t bytes = 0, total_n = 0;
+      while (!pending.empty()) {
+        auto &r = pending.front();
+        const uint64_t b = request_bytes(r->n);
+        if (bytes_in_use + bytes + b > budget && !batch.empty()) break;
+        if (bytes_in_use + bytes + b > budget && bytes_in_use > 0) break;
+        bytes += b;
+        total_n += r->n;
+        batch.push_back(r);
+        pending.pop_front();
+      }
+      if (!batch.empty()) {
+        std::vector<JobSpec> specs(batch.size());
+        uint64_t maxn = 0, first = 0;
+        for (auto &r : batch) maxn = std::max(maxn, r->n);
+        const Cfg big = resolve_cfg(cx, maxn, nullptr);
+        for (size_t j = 0; j < batch.size(); j++) {
+          specs[j] = {batch[j]->n, batch[j]->base_off, first, resolve_cfg(cx, batch[j]->n, nullptr)};
+          specs[j].cfg.seg_len = big.seg_len;
+          specs[j].cfg.red_log2 = big.red_log2;
+          first += batch[j]->n;
+        }
+        Slot &sl = *free_slot;
+        int rc = build_plan(specs, sl.plan);
+        if (!rc && sl.scal.ensure(std::max<uint64_t>(first, 1) * 32) != cudaSuccess)
+          rc = fail(ERR_CUDA, "server scalar buffer allocation failed");
+        if (!rc) {
+          uint64_t off = 0;
+          for (auto &r : batch) {
+            if (r->n)
+              cudaMemcpyAsync((char *)sl.scal.p + off * 32, r->scalars.data(), r->n * 32,
+                              cudaMemcpyHostToDevice, sl.st);
+            off += r->n;
+          }
+          rc = enqueue_pass(cx, sl.ws, sl.plan, sl.scal.p, sl.st, false, false, 0);
+        }
+        if (!rc) rc = cudaEventRecord(sl.done, sl.st) == cudaSuccess ? 0 : ERR_CUDA;
+        if (rc) {
+          for (auto &r : batch) {
+            r->status = rc;
+            r->t_done = std::chrono::steady_clock::now();
+          }
+          cv_done.notify_all();
+        } else {
+          sl.busy = true;
+          sl.bytes = bytes;
+          sl.reqs = batch;
+          bytes_in_use += bytes;
+          stats.passes++;
+          stats.bytes_peak = std::max(stats.bytes_peak, bytes_in_use);
+          uint64_t inflight = 0;
+          for (auto &s2 : slots) inflight += s2->busy;
+          stats.inflight_peak = std::max(stats.inflight_peak, inflight);
+        }
+        continue;
+      }
+    }
+    bool busy = false;
+    for (auto &sl : slots) busy |= sl->busy;
+    if (busy) {
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(50));
+      lk.lock();
+    } else {
+      cv.wait_for(lk, std::chrono::milliseconds(5));
+    }
+  }
+}
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+int msm_last_error(char *buf, size_t len) {
+  if (buf && len) {
+    strncpy(buf, g_msg, len - 1);
+    buf[len - 1] = 0;
+  }
+  return g_err;
+}
+
+void *msm_init(const char *xclbin, ssize_t xclbin_len, const g1_affine_t *points, ssize_t npoints) {
+  (void)xclbin;
+  (void)xclbin_len;
+  g_err = 0;
+  g_msg[0] = 0;
+  if (npoints < 0 || (npoints > 0 && !points)) {
+    fail(ERR_ARG, "msm_init: bad point array");
+    return nullptr;
+  }
+  if ((uint64_t)npoints >= (1ull << 31)) {
+    fail(ERR_ARG, "msm_init: at most 2^31 - 1 points");
+    return nullptr;
+  }
+  auto *cx = new Ctx();
+  if (init_device(cx) || load_bases(cx, points, (uint64_t)npoints)) {
+    fprintf(stderr, "msm_init: %s\n", g_msg);
+    delete cx;
+    return nullptr;
+  }
+  return cx;
+}
+
+void msm_free(void *context) { delete (Ctx *)context; }
+
+int msm_mult_ex(void *context, g1_projective_t *out, uint64_t batch_size,
+                const biginteger256_t *scalars, const msm_options_t *opt) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || (batch_size && (!out || !scalars))) return fail(ERR_ARG, "msm_mult: null argument");
+  std::lock_guard<std::mutex> lk(cx->mu);
+  if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
+  std::vector<uint64_t> sizes(batch_size, cx->npoints), offs(batch_size, 0);
+  int rc = run_msms(cx, out, sizes, offs, scalars, nullptr, opt);
+  if (rc && out) memset(out, 0, batch_size * sizeof(g1_projective_t));
+  return rc;
+}
+
+void msm_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+              const biginteger256_t *scalars) {
+  if (msm_mult_ex(context, out, batch_size, scalars, nullptr))
+    fprintf(stderr, "msm_mult: %s\n", g_msg);
+}
+
+int msm_mult_uneven(void *context, g1_projective_t *out, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const biginteger256_t *scalars,
+                    const msm_options_t *opt) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || (num_msms && (!out || !sizes || !scalars)))
+    return fail(ERR_ARG, "msm_mult_uneven: null argument");
+  std::lock_guard<std::mutex> lk(cx->mu);
+  if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
+  std::vector<uint64_t> sz(sizes, sizes + num_msms), of(num_msms, 0);
+  if (base_offsets) of.assign(base_offsets, base_offsets + num_msms);
+  int rc = run_msms(cx, out, sz, of, scalars, nullptr, opt);
+  if (rc && out) memset(out, 0, num_msms * sizeof(g1_projective_t));
+  return rc;
+}
+
+int msm_mult_device(void *context, g1_projective_t *out, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const void *d_scalars, const msm_options_t *opt) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || (num_msms && (!out || !sizes || !d_scalars)))
+    return fail(ERR_ARG, "msm_mult_device: null argument");
+  std::lock_guard<std::mutex> lk(cx->mu);
+  if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
+  std::vector<uint64_t> sz(sizes, sizes + num_msms), of(num_msms, 0);
+  if (base_offsets) of.assign(base_offsets, base_offsets + num_msms);
+  int rc = run_msms(cx, out, sz, of, nullptr, d_scalars, opt);
+  if (rc && out) memset(out, 0, num_msms * sizeof(g1_projective_t));
+  return rc;
+}
+
+int msm_get_config(void *context, uint64_t npoints, msm_options_t *out) {
+  auto *cx = (Ctx *)context;
+  if (!cx || !out) return fail(ERR_ARG, "msm_get_config: null argument");
+  const Cfg c = resolve_cfg(cx, npoints, nullptr);
+  out->window_bits = (int32_t)c.c;
+  out->signed_digits = c.signed_digits ? 1 : 2;
+  out->seg_len = (int32_t)c.seg_len;
+  out->red_len_log2 = (int32_t)c.red_log2;
+  out->use_graph = 0;
+  out->mode = 1;
+  return 0;
+}
+
+int msm_set_timing(void *context, int32_t enable) {
+  auto *cx = (Ctx *)context;
+  if (!cx) return fail(ERR_ARG, "null context");
+  std::lock_guard<std::mutex> lk(cx->mu);
+  cx->timing = enable != 0;
+  return 0;
+}
+
+int msm_last_timings(void *context, double *ms, int32_t max_stages) {
+  auto *cx = (Ctx *)context;
+  if (!cx || !ms) return fail(ERR_ARG, "null argument");
+  const int n = std::min<int>(max_stages, MSM_NUM_STAGES);
+  for (int k = 0; k < n; k++) ms[k] = cx->last_ms[k];
+  return n;
+}
+
+int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats) {
+  auto *cx = (Ctx *)context;
+  if (!cx || !stats) return fail(ERR_ARG, "null argument");
+  const int n = std::min<int>(max_stats, 4);
+  for (int k = 0; k < n; k++) stats[k] = cx->last_stats[k];
+  return n;
+}
+
+int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *best_out) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || npoints == 0 || npoints > cx->npoints) return fail(ERR_ARG, "msm_tune: bad size");
+  if (budget_ms <= 0) budget_ms = 20000;
+  std::vector<biginteger256_t> sc(npoints);
+  for (uint64_t i = 0; i < npoints; i++) uniform_scalar(0x7475e3ull, i, sc[i].data);
+  const Cfg h = heuristic_cfg(npoints);
+  std::vector<Cfg> cands;
+  for (int dc = -2; dc <= 2; dc++) {
+    const int c = (int)h.c + dc;
+    if (c < 6 || c > 21) continue;
+    for (uint32_t sg : {1u, 0u}) {
+      if (!sg && dc != 0) continue;
+      msm_options_t o{};
+      o.window_bits = c;
+      o.signed_digits = sg ? 1 : 2;
+      Cfg cf = resolve_cfg(cx, npoints, &o);
+      cands.push_back(cf);
+      if (sg && dc == 0) {
+        Cfg cf2 = cf;
+        cf2.seg_len = std::max<uint32_t>(32, cf.seg_len / 4);
+        cands.push_back(cf2);
+      }
+    }
+  }
+  std::lock_guard<std::mutex> lk(cx->mu);
+  if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
+  DevBuf dsc;
+  CK(dsc.ensure(npoints * 32));
+  CK(cudaMemcpy(dsc.p, sc.data(), npoints * 32, cudaMemcpyHostToDevice));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const auto t_start = std::chrono::steady_clock::now();
+  double best_ms = 1e300;
+  Cfg best = h;
+  for (const Cfg &cf : cands) {
+    std::vector<JobSpec> one(1);
+    one[0] = {npoints, 0, 0, cf};
+    Plan pl;
+    if (build_plan(one, pl)) continue;
+    double t = 1e300;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, cx->stream);
+      if (enqueue_pass(cx, cx->ws, pl, dsc.p, cx->stream, false, false, 0)) break;
+      cudaEventRecord(e1, cx->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) t = std::min(t, (double)ms);
+    }
+    if (t < best_ms) {
+      best_ms = t;
+      best = cf;
+    }
+    const double spent = std::chrono::duration<double, std::milli>(
+                             std::chrono::steady_clock::now() - t_start).count();
+    if (spent > budget_ms) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cx->tuned[log2_ceil(npoints)] = best;
+  if (const char *path = getenv("MSM_TUNE_CACHE")) {
+    if (FILE *f = fopen(path, "a")) {
+      fprintf(f, "%u %u %u %u %u %.4f\n", log2_ceil(npoints), best.c, best.signed_digits,
+              best.seg_len, best.red_log2, best_ms);
+      fclose(f);
+    }
+  }
+  if (best_out) {
+    best_out->window_bits = (int32_t)best.c;
+    best_out->signed_digits = best.signed_digits ? 1 : 2;
+    best_out->seg_len = (int32_t)best.seg_len;
+    best_out->red_len_log2 = (int32_t)best.red_log2;
+    best_out->use_graph = 0;
+    best_out->mode = 1;
+  }
+  return 0;
+}
+
+void *msm_server_create(void *context, uint64_t hbm_budget_bytes, int32_t max_inflight) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || max_inflight <= 0) {
+    fail(ERR_ARG, "msm_server_create: bad argument");
+    return nullptr;
+  }
+  auto *sv = new Server();
+  sv->cx = cx;
+  sv->budget = hbm_budget_bytes;
+  sv->max_inflight = max_inflight;
+  for (int i = 0; i < max_inflight; i++) {
+    auto sl = std::make_unique<Slot>();
+    if (cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
+      fail(ERR_CUDA, "msm_server_create: stream creation failed");
+      delete sv;
+      return nullptr;
+    }
+    sv->slots.push_back(std::move(sl));
+  }
+  sv->worker = std::thread([sv] {
+    cudaSetDevice(sv->cx->device);
+    sv->loop();
+  });
+  return sv;
+}
+
+int64_t msm_server_submit(void *server, const biginteger256_t *scalars, uint64_t n,
+                          uint64_t base_offset) {
+  auto *sv = (Server *)server;
+  if (!sv || (n && !scalars)) return fail(ERR_ARG, "msm_server_submit: null argument");
+  if (base_offset > sv->cx->npoints || n > sv->cx->npoints - base_offset)
+    return fail(ERR_ARG, "msm_server_submit: bases outside the resident set");
+  const uint64_t need = sv->request_bytes(n);
+  if (need > sv->budget)
+    return fail(ERR_BUDGET, "request of %llu points needs %llu bytes, over the %llu byte budget",
+                (unsigned long long)n, (unsigned long long)need, (unsigned long long)sv->budget);
+  auto r = std::make_shared<Request>();
+  r->n = n;
+  r->base_off = base_offset;
+  r->scalars.assign(scalars, scalars + n);
+  r->t_submit = std::chrono::steady_clock::now();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  r->id = sv->next_id++;
+  sv->all[r->id] = r;
+  sv->pending.push_back(r);
+  sv->stats.submitted++;
+  sv->cv.notify_all();
+  return r->id;
+}
+
+int msm_server_poll(void *server, int64_t id, g1_projective_t *out, int32_t wait_ms,
+                    double *latency_ms) {
+  auto *sv = (Server *)server;
+  if (!sv) return fail(ERR_ARG, "null server");
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->all.find(id);
+  if (it == sv->all.end()) return fail(ERR_ARG, "unknown request id %lld", (long long)id);
+  auto r = it->second;
+  if (r->status == 1 && wait_ms > 0)
+    sv->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return r->status != 1; });
+  if (r->status == 1) return 1;
+  if (r->status < 0) return fail(r->status, "request %lld failed", (long long)id);
+  if (out) memcpy(out, r->result, MSM_PROJ_BYTES);
+  if (latency_ms)
+    *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  sv->all.erase(it);
+  return 0;
+}
+
+int msm_server_stats(void *server, msm_server_stats_t *st) {
+  auto *sv = (Server *)server;
+  if (!sv || !st) return fail(ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  *st = sv->stats;
+  st->bytes_in_use = sv->bytes_in_use;
+  return 0;
+}
+
+void msm_server_destroy(void *server) {
+  auto *sv = (Server *)server;
+  if (!sv) return;
+  sv->stop = true;
+  sv->cv.notify_all();
+  if (sv->worker.joinable()) sv->worker.join();
+  for (auto &sl : sv->slots) {
+    if (sl->st) {
+      cudaStreamSynchronize(sl->st);
+      cudaStreamDestroy(sl->st);
+    }
+    if (sl->done) cudaEventDestroy(sl->done);
+  }
+  delete sv;
+}
+
+int msm_generate_bases(uint64_t seed, uint64_t first, uint64_t n, g1_affine_t *out) {
+  g_err = 0;
+  if (n && !out) return fail(ERR_ARG, "null output");
+  const char *dev = getenv("MSM_DEVICE");
+  CK(cudaSetDevice(dev ? atoi(dev) : 0));
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  DevBuf table, buf;
+  int rc = 0;
+  if (table.ensure(2048 * MSM_BASE_BYTES) != cudaSuccess) rc = fail(ERR_CUDA, "alloc failed");
+  if (!rc && msm_build_gen_table(table.as<uint4>(), st) != cudaSuccess)
+    rc = fail(ERR_CUDA, "table launch failed");
+  const uint64_t chunk = std::min<uint64_t>(std::max<uint64_t>(n, 1), 1ull << 22);
+  if (!rc && buf.ensure(chunk * MSM_AFFINE_BYTES) != cudaSuccess) rc = fail(ERR_CUDA, "alloc failed");
+  for (uint64_t i0 = 0; !rc && i0 < n; i0 += chunk) {
+    const uint64_t k = std::min(chunk, n - i0);
+    if (msm_launch_gen_bases(seed, first + i0, k, buf.p, table.as<uint4>(), st) != cudaSuccess ||
+        cudaMemcpyAsync(out + i0, buf.p, k * MSM_AFFINE_BYTES, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = fail(ERR_CUDA, "base generation failed: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+int msm_generate_scalars(uint64_t seed, uint64_t n, int32_t kind, uint64_t msm_index,
+                         biginteger256_t *out) {
+  if (n && !out) return fail(ERR_ARG, "null output");
+  if (kind != 0 && kind != 1) return fail(ERR_ARG, "unknown scalar kind %d", kind);
+  const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nt; t++) {
+    th.emplace_back([=] {
+      const uint64_t a = n * t / nt, b = n * (t + 1) / nt;
+      for (uint64_t i = a; i < b; i++) {
+        if (kind == 0) uniform_scalar(seed, i, out[i].data);
+        else mixed_scalar(seed, msm_index, i, out[i].data);
+      }
+    });
+  }
+  for (auto &t : th) t.join();
+  return 0;
+}
+
+double msm_measure_imad_peak(int32_t iters) {
+  const char *dev = getenv("MSM_DEVICE");
+  if (cudaSetDevice(dev ? atoi(dev) : 0) != cudaSuccess) return -1;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev ? atoi(dev) : 0) != cudaSuccess) return -1;
+  if (iters <= 0) iters = 20000;
+  DevBuf sink;
+  if (sink.ensure(16) != cudaSuccess) return -1;
+  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(e0);
+    msm_launch_imad_peak(sink.as<uint32_t>(), blocks, threads, iters, 0);
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double ops = (double)blocks * threads * iters * 16.0;
+    if (rep > 0) best = std::max(best, ops / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+double msm_measure_madd_rate(void *context, int32_t iters) {
+  auto *cx = (Ctx *)context;
+  if (!cx || cx->npoints == 0) return -1;
+  std::lock_guard<std::mutex> lk(cx->mu);
+  cudaSetDevice(cx->device);
+  if (iters <= 0) iters = 2000;
+  const int threads = 256, blocks = cx->num_sms * 2;
+  DevBuf out;
+  if (out.ensure((size_t)blocks * threads * MSM_BUCKET_BYTES) != cudaSuccess) return -1;
+  const uint32_t nb = (uint32_t)std::min<uint64_t>(cx->npoints, 1u << 16);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(e0, cx->stream);
+    msm_launch_madd_bench(cx->bases.as<uint4>(), nb, out.as<uint4>(), blocks, threads, iters,
+                          cx->stream);
+    cudaEventRecord(e1, cx->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0) best = std::max(best, (double)blocks * threads * iters / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+int msm_device_info(char *buf, size_t len) {
+  const char *dev = getenv("MSM_DEVICE");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, dev ? atoi(dev) : 0));
+  int clk = 0;
+  cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, dev ? atoi(dev) : 0);
+  if (buf && len)
+    snprintf(buf, len, "%s; sm_%d%d; %d SMs; %d MHz max SM clock; %.1f GiB", prop.name,
+             prop.major, prop.minor, prop.multiProcessorCount, clk / 1000,
+             prop.totalGlobalMem / 1073741824.0);
+  return 0;
+}
+
+int msm_field_selftest(int32_t op, const uint32_t *a, const uint32_t *b, uint32_t *out, uint64_t n) {
+  g_err = 0;
+  if (n && (!a || !b || !out)) return fail(ERR_ARG, "null argument");
+  const char *dev = getenv("MSM_DEVICE");
+  CK(cudaSetDevice(dev ? atoi(dev) : 0));
+  DevBuf da, db, dout;
+  const size_t bytes = std::max<uint64_t>(n, 1) * 48;
+  CK(da.ensure(bytes));
+  CK(db.ensure(bytes));
+  CK(dout.ensure(bytes));
+  CK(cudaMemcpy(da.p, a, n * 48, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(db.p, b, n * 48, cudaMemcpyHostToDevice));
+  CK(msm_launch_field_test(op, da.as<uint32_t>(), db.as<uint32_t>(), dout.as<uint32_t>(), n, 0));
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(out, dout.p, n * 48, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,547 @@
+// The MSM pipeline of one pass (one or many MSMs sharing one sort), all on the device:
+//
+//   1. k_count     signed c-bit digits of every scalar, histogram of (MSM, window, |digit|) keys
+//   2. k_scan_*    exclusive scans -> bucket offsets in the sorted array and task offsets
+//   3. k_scatter   counting-sort scatter of (base index | sign) into bucket order
+//   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
+//   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
+//   6. k_merge     buckets split over several runs: warp-parallel sum of their partials
+//   7. k_reduce1   per window segment: running sum R and triangle sum A (pippenger.h:25-33)
+//   8. k_reduce2   per window: combine segments -> window sum
+//   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
+//                  Weierstrass, add the bases without a twisted-Edwards image
+//                  (driver.cpp:349-372), write g1_projective_t (bls12_377_g1.h:427-439, 667-690)
+//
+// Every launch has a shape fixed by the host plan; data-dependent sizes (tasks, heavy buckets)
+// are read from device counters, so a pass can be captured in a CUDA graph and replayed.
+#include "engine.h"
+#include "curve.cuh"
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ void set_error(uint32_t *counters, uint32_t code, uint32_t info) {
+  if (atomicCAS(&counters[CNT_ERROR], 0u, code) == 0u) counters[CNT_ERROR_INFO] = info;
+}
+
+__device__ __forceinline__ uint32_t find_job(const JobDesc *jobs, uint32_t n_jobs, uint64_t g) {
+  uint32_t lo = 0, hi = n_jobs;  // last job with point_begin <= g
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (jobs[mid].point_begin <= g) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// scalar as 8 little-endian words plus a zero guard word, masked to 253 bits
+struct ScalarBits {
+  uint32_t w[9];
+};
+
+__device__ __forceinline__ ScalarBits load_scalar(const uint4 *p) {
+  const uint4 a = p[0], b = p[1];
+  ScalarBits s;
+  s.w[0] = a.x; s.w[1] = a.y; s.w[2] = a.z; s.w[3] = a.w;
+  s.w[4] = b.x; s.w[5] = b.y; s.w[6] = b.z; s.w[7] = b.w & 0x1fffffffu;
+  s.w[8] = 0;
+  return s;
+}
+
+__device__ __forceinline__ uint32_t slice_bits(const ScalarBits &s, uint32_t off, uint32_t c) {
+  const uint32_t k = off >> 5;
+  const uint64_t two = ((uint64_t)s.w[k < 8 ? k + 1 : 8] << 32) | s.w[k < 9 ? k : 8];
+  return (uint32_t)(two >> (off & 31)) & ((1u << c) - 1u);
+}
+
+// Digit of window w given the running carry (hardcaml/test/top/utils.ml:243-288): slice + carry;
+// below the top window a value >= 2^(c-1) becomes value - 2^c with carry 1.  Returns the signed
+// digit and updates carry.  Unsigned mode returns the plain slice.
+__device__ __forceinline__ int32_t window_digit(const ScalarBits &s, const JobDesc &jd, uint32_t w,
+                                                uint32_t &carry) {
+  const uint32_t off = w * jd.c;
+  const uint32_t width = min(jd.c, (uint32_t)MSM_SCALAR_BITS - off);
+  int32_t d = (int32_t)(slice_bits(s, off, width) + carry);
+  if (!jd.signed_digits) return d;
+  if (w + 1 < jd.nwin && d >= (int32_t)(1u << (jd.c - 1))) {
+    d -= (int32_t)(1u << jd.c);
+    carry = 1;
+  } else {
+    carry = 0;
+  }
+  return d;
+}
+
+__device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, uint32_t mag) {
+  return jd.bucket_begin + w * jd.nb + (mag - 1u);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 1. histogram
+// ---------------------------------------------------------------------------------------------
+__global__ void k_count(PassBuffers pb) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= pb.n_points) return;
+  const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
+  const JobDesc jd = pb.jobs[j];
+  const uint64_t i = g - jd.point_begin;
+  if (pb.flags[jd.base_off + i] != BASE_OK) return;
+  const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
+  uint32_t carry = 0;
+  for (uint32_t w = 0; w < jd.nwin; w++) {
+    const int32_t d = window_digit(s, jd, w, carry);
+    if (d == 0) continue;
+    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&pb.count[key], (uint32_t)__popc(peers));
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 2. scans of (count, ceil(count / seg_len))
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint2 warp_incl_scan2(uint2 v) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t a = __shfl_up_sync(0xffffffffu, v.x, o);
+    const uint32_t b = __shfl_up_sync(0xffffffffu, v.y, o);
+    if ((int)(threadIdx.x & 31) >= o) { v.x += a; v.y += b; }
+  }
+  return v;
+}
+
+// block-wide exclusive scan of pairs; returns this thread's exclusive prefix and the block total
+__device__ __forceinline__ uint2 block_excl_scan2(uint2 v, uint2 &total) {
+  __shared__ uint2 warp_tot[32];
+  __shared__ uint2 tot_sh;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  const uint2 inc = warp_incl_scan2(v);
+  if (lane == 31) warp_tot[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const uint2 t = lane < nw ? warp_tot[lane] : make_uint2(0, 0);
+    const uint2 ti = warp_incl_scan2(t);
+    if (lane < nw) warp_tot[lane] = make_uint2(ti.x - t.x, ti.y - t.y);
+    if (lane == 31) tot_sh = ti;
+  }
+  __syncthreads();
+  total = tot_sh;
+  const uint2 base = warp_tot[wid];
+  __syncthreads();  // the shared words are reused by the next call
+  return make_uint2(base.x + inc.x - v.x, base.y + inc.y - v.y);
+}
+
+__device__ __forceinline__ uint32_t ntask_of(uint32_t cnt, uint32_t seg_len) {
+  return (cnt + seg_len - 1) / seg_len;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(PassBuffers pb) {
+  const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  uint2 v = make_uint2(0, 0);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < pb.n_buckets) {
+      const uint32_t c = pb.count[base + k];
+      v.x += c;
+      v.y += ntask_of(c, pb.seg_len);
+    }
+  }
+  uint2 total;
+  block_excl_scan2(v, total);
+  if (threadIdx.x == 0) {
+    pb.scan_tmp[2 * blockIdx.x] = total.x;
+    pb.scan_tmp[2 * blockIdx.x + 1] = total.y;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(PassBuffers pb, uint32_t nblk) {
+  // one block: exclusive scan of the per-block totals, in chunks of kScanThreads
+  __shared__ uint2 carry_sh;
+  if (threadIdx.x == 0) carry_sh = make_uint2(0, 0);
+  __syncthreads();
+  for (uint32_t c0 = 0; c0 < nblk; c0 += kScanThreads) {
+    const uint32_t i = c0 + threadIdx.x;
+    const uint2 v = i < nblk ? make_uint2(pb.scan_tmp[2 * i], pb.scan_tmp[2 * i + 1]) : make_uint2(0, 0);
+    uint2 total;
+    const uint2 ex = block_excl_scan2(v, total);
+    const uint2 cr = carry_sh;
+    if (i < nblk) {
+      pb.scan_tmp[2 * i] = cr.x + ex.x;
+      pb.scan_tmp[2 * i + 1] = cr.y + ex.y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry_sh = make_uint2(cr.x + total.x, cr.y + total.y);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const uint2 t = carry_sh;
+    if ((uint64_t)t.x > pb.max_entries) set_error(pb.counters, 1, t.x);
+    if (t.y > pb.max_tasks) set_error(pb.counters, 2, t.y);
+    pb.counters[CNT_TASKS] = min(t.y, pb.max_tasks);
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(PassBuffers pb) {
+  const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
+  uint32_t c[kScanItems];
+  uint2 v = make_uint2(0, 0);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    c[k] = base + k < pb.n_buckets ? pb.count[base + k] : 0u;
+    v.x += c[k];
+    v.y += ntask_of(c[k], pb.seg_len);
+  }
+  uint2 total;
+  uint2 ex = block_excl_scan2(v, total);
+  ex.x += pb.scan_tmp[2 * blockIdx.x];
+  ex.y += pb.scan_tmp[2 * blockIdx.x + 1];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < pb.n_buckets) {
+      pb.offset[base + k] = ex.x;
+      pb.taskoff[base + k] = ex.y;
+    }
+    ex.x += c[k];
+    ex.y += ntask_of(c[k], pb.seg_len);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 3. scatter into bucket order
+// ---------------------------------------------------------------------------------------------
+__global__ void k_scatter(PassBuffers pb) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= pb.n_points) return;
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
+  const JobDesc jd = pb.jobs[j];
+  const uint64_t i = g - jd.point_begin;
+  const uint64_t bidx = jd.base_off + i;
+  if (pb.flags[bidx] != BASE_OK) return;
+  const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
+  const int lane = threadIdx.x & 31;
+  uint32_t carry = 0;
+  for (uint32_t w = 0; w < jd.nwin; w++) {
+    const int32_t d = window_digit(s, jd, w, carry);
+    if (d == 0) continue;
+    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t basepos = 0;
+    if (lane == leader) basepos = atomicAdd(&pb.fill[key], (uint32_t)__popc(peers));
+    basepos = __shfl_sync(peers, basepos, leader);
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    const uint64_t pos = (uint64_t)pb.offset[key] + basepos + rank;
+    if (pos < pb.max_entries) {
+      pb.vals[pos] = (uint32_t)bidx | (d < 0 ? 0x80000000u : 0u);
+    } else {
+      set_error(pb.counters, 3, (uint32_t)pos);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 4. tasks
+// ---------------------------------------------------------------------------------------------
+__global__ void k_tasks(PassBuffers pb) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= pb.n_buckets) return;
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t cnt = pb.count[b];
+  if (cnt == 0) return;
+  const uint32_t nt = ntask_of(cnt, pb.seg_len);
+  const uint32_t t0 = pb.taskoff[b];
+  const uint32_t off = pb.offset[b];
+  for (uint32_t k = 0; k < nt; k++) {
+    const uint32_t t = t0 + k;
+    if (t >= pb.max_tasks) { set_error(pb.counters, 4, t); return; }
+    Task tk;
+    tk.start = off + k * pb.seg_len;
+    tk.len = min(pb.seg_len, cnt - k * pb.seg_len);
+    tk.bucket = b;
+    tk.pad = 0;
+    pb.tasks[t] = tk;
+  }
+  if (nt > 1) pb.heavy[atomicAdd(&pb.counters[CNT_HEAVY], 1u)] = b;
+}
+
+// ---------------------------------------------------------------------------------------------
+// 5. bucket accumulation (persistent; warps fetch 32 tasks at a time)
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_accumulate(PassBuffers pb) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t ntasks = pb.counters[CNT_TASKS];
+  if (pb.counters[CNT_ERROR]) return;
+  for (;;) {
+    uint32_t first = 0;
+    if (lane == 0) first = atomicAdd(&pb.counters[CNT_TASK_CURSOR], 32u);
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if (first >= ntasks) break;
+    const uint32_t t = first + lane;
+    if (t < ntasks) {
+      const Task tk = pb.tasks[t];
+      xyzt_t acc = xyzt_identity();
+      for (uint32_t e = 0; e < tk.len; e++) {
+        const uint32_t v = pb.vals[tk.start + e];
+        const uint32_t idx = v & 0x7fffffffu;
+        if (idx >= pb.n_bases) {  // cannot happen for a consistent sort; never read out of bounds
+          set_error(pb.counters, 5, idx);
+          break;
+        }
+        pre_t b;
+        pre_load(b, pb.bases + (size_t)idx * 9);
+        acc = te_madd(acc, b, (v >> 31) != 0);
+      }
+      xyzt_store(pb.partials + (size_t)t * 12, acc);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 6. buckets spread over several tasks: one warp sums the partials
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ xyzt_t shfl_down_xyzt(const xyzt_t &p, int off) {
+  xyzt_t r;
+#pragma unroll
+  for (int k = 0; k < FQ_LIMBS; k++) {
+    r.x.v[k] = __shfl_down_sync(0xffffffffu, p.x.v[k], off);
+    r.y.v[k] = __shfl_down_sync(0xffffffffu, p.y.v[k], off);
+    r.z.v[k] = __shfl_down_sync(0xffffffffu, p.z.v[k], off);
+    r.t.v[k] = __shfl_down_sync(0xffffffffu, p.t.v[k], off);
+  }
+  return r;
+}
+
+__device__ __forceinline__ xyzt_t warp_sum_xyzt(xyzt_t acc) {
+#pragma unroll 1
+  for (int off = 16; off > 0; off >>= 1) {
+    const xyzt_t o = shfl_down_xyzt(acc, off);
+    acc = te_add_ool(acc, o);  // lanes >= 32 - off add garbage-free copies; only lane 0 is used
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t nheavy = pb.counters[CNT_HEAVY];
+  const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t h = warp_global; h < nheavy; h += nwarps) {
+    const uint32_t b = pb.heavy[h];
+    const uint32_t nt = ntask_of(pb.count[b], pb.seg_len);
+    const uint32_t t0 = pb.taskoff[b];
+    xyzt_t acc = xyzt_identity();
+    for (uint32_t k = lane; k < nt; k += 32) {
+      xyzt_t p;
+      xyzt_load(p, pb.partials + (size_t)(t0 + k) * 12);
+      acc = te_add_ool(acc, p);
+    }
+    acc = warp_sum_xyzt(acc);
+    __syncwarp();
+    if (lane == 0) xyzt_store(pb.partials + (size_t)t0 * 12, acc);
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// 7. level-1 reduction: per segment of 2^red_len_log2 buckets, from the top bucket down,
+//    running R += B_b and A += R (triangleSumUpdate, pippenger.h:25-33)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_win(const WinDesc *wins, uint32_t n_wins, uint32_t s) {
+  uint32_t lo = 0, hi = n_wins;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (wins[mid].seg_begin <= s) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= pb.n_segs) return;
+  if (pb.counters[CNT_ERROR]) return;
+  const WinDesc wd = pb.wins[find_win(pb.wins, pb.n_wins, s)];
+  const uint32_t L = 1u << pb.red_len_log2;
+  const uint32_t lo = (s - wd.seg_begin) * L;
+  const uint32_t hi = min(lo + L, wd.nb);
+  xyzt_t R = xyzt_identity(), A = xyzt_identity();
+  bool r_live = false, a_live = false;
+  for (uint32_t b = hi; b-- > lo;) {
+    const uint32_t gb = wd.bucket_begin + b;
+    if (pb.count[gb] != 0) {
+      xyzt_t B;
+      xyzt_load(B, pb.partials + (size_t)pb.taskoff[gb] * 12);
+      R = r_live ? te_add_ool(R, B) : B;
+      r_live = true;
+    }
+    if (r_live) {
+      A = a_live ? te_add_ool(A, R) : R;
+      a_live = true;
+    }
+  }
+  xyzt_store(pb.seg_out + (size_t)s * 24, R);
+  xyzt_store(pb.seg_out + (size_t)s * 24 + 12, A);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 8. level-2 reduction: one block per window.  Window sum = sum_s A_s + L * sum_s s * R_s;
+//    thread t takes a contiguous run of segments starting at s0 and contributes
+//    SA + L * (T + s0 * RR) with SA = sum A_s, RR = sum R_s, T = sum (s - s0) R_s; the block
+//    then sums the contributions in a shared-memory tree.
+// ---------------------------------------------------------------------------------------------
+constexpr int kRed2Threads = 128;
+
+__global__ void __launch_bounds__(kRed2Threads) k_reduce2(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t gw = blockIdx.x;
+  if (gw >= pb.n_wins) return;
+  __shared__ uint4 sh[kRed2Threads * 12];
+  const WinDesc wd = pb.wins[gw];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t per = (wd.nseg + kRed2Threads - 1) / kRed2Threads;
+  const uint32_t s0 = tid * per;
+  const uint32_t s1 = min(s0 + per, wd.nseg);
+  xyzt_t X = xyzt_identity();
+  if (s0 < s1) {
+    xyzt_t SA = xyzt_identity(), T = xyzt_identity(), RR = xyzt_identity();
+    for (uint32_t s = s1; s-- > s0;) {
+      T = te_add_ool(T, RR);
+      xyzt_t R, A;
+      xyzt_load(R, pb.seg_out + (size_t)(wd.seg_begin + s) * 24);
+      xyzt_load(A, pb.seg_out + (size_t)(wd.seg_begin + s) * 24 + 12);
+      RR = te_add_ool(RR, R);
+      SA = te_add_ool(SA, A);
+    }
+    X = s0 > 0 ? te_add_ool(T, te_mul_small(RR, s0)) : T;
+#pragma unroll 1
+    for (uint32_t k = 0; k < pb.red_len_log2; k++) X = te_dbl_ool(X);
+    X = te_add_ool(X, SA);
+  }
+  xyzt_store(sh + tid * 12, X);
+  __syncthreads();
+#pragma unroll 1
+  for (uint32_t stride = kRed2Threads / 2; stride > 0; stride >>= 1) {
+    if (tid < stride) {
+      xyzt_t o;
+      xyzt_load(o, sh + (tid + stride) * 12);
+      X = te_add_ool(X, o);
+      xyzt_store(sh + tid * 12, X);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) xyzt_store(pb.win_sum + (size_t)gw * 12, X);
+}
+
+// ---------------------------------------------------------------------------------------------
+// 9. per MSM: window combine, Weierstrass map, special bases, ABI output
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void load_class_point(wpt_t &p, const uint4 *cp) {
+  fq_load(p.x, cp);
+  fq_load(p.y, cp + 3);
+  p.z = fq_one();
+}
+
+__global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
+  const uint32_t j = blockIdx.x;
+  if (j >= pb.n_jobs) return;
+  const JobDesc jd = pb.jobs[j];
+  __shared__ uint32_t cls_sum[8];
+  if (threadIdx.x < 8) cls_sum[threadIdx.x] = 0;
+  __syncthreads();
+  // multiples of the special bases: every special base has order 2 or 4 (y = 0, or
+  // Montgomery u = -1), so k * P = (k mod 4) * P
+  for (uint32_t s = threadIdx.x; s < pb.n_special; s += blockDim.x) {
+    const uint32_t idx = pb.special_idx[s];
+    if (idx < jd.base_off || idx >= jd.base_off + jd.n) continue;
+    const uint4 w0 = pb.scalars[2 * (jd.scalar_off + (idx - jd.base_off))];
+    atomicAdd(&cls_sum[pb.special_cls[s] & 7], w0.x & 3u);
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  uint64_t *out = pb.results + (size_t)jd.result_slot * 18;
+  if (pb.counters[CNT_ERROR]) {
+    for (int k = 0; k < 18; k++) out[k] = 0;
+    return;
+  }
+  xyzt_t acc = xyzt_identity();
+  if (jd.n > 0 && jd.nwin > 0) {
+    xyzt_load(acc, pb.win_sum + (size_t)(jd.win_begin + jd.nwin - 1) * 12);
+#pragma unroll 1
+    for (int w = (int)jd.nwin - 2; w >= 0; w--) {
+#pragma unroll 1
+      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_ool(acc);
+      xyzt_t ws;
+      xyzt_load(ws, pb.win_sum + (size_t)(jd.win_begin + w) * 12);
+      acc = te_add_ool(acc, ws);
+    }
+  }
+  wpt_t res = te_to_weierstrass(acc);
+  for (uint32_t c = 0; c < pb.n_classes && c < 8; c++) {
+    const uint32_t m = cls_sum[c] & 3u;
+    if (m == 0) continue;
+    wpt_t p;
+    load_class_point(p, pb.class_pts + c * 6);
+    for (uint32_t k = 0; k < m; k++) res = w_add(res, p);
+  }
+  res = w_normalize(res);
+  // g1_projective_t {x[6], y[6], z[6]}: (x*R, y*R, R) or arkworks' zero() (R, R, 0)
+  const fq_t one = fq_canon(fq_one());
+  const bool inf = fq_is_zero(res.z);
+  const fq_t ox = inf ? one : res.x;
+  const fq_t oy = inf ? one : res.y;
+  const fq_t oz = inf ? fq_zero() : one;
+  for (int k = 0; k < 6; k++) {
+    out[k] = ((uint64_t)ox.v[2 * k + 1] << 32) | ox.v[2 * k];
+    out[6 + k] = ((uint64_t)oy.v[2 * k + 1] << 32) | oy.v[2 * k];
+    out[12 + k] = ((uint64_t)oz.v[2 * k + 1] << 32) | oz.v[2 * k];
+  }
+}
+
+}  // namespace
+
+size_t msm_scan_tmp_words(uint32_t n_buckets) {
+  return 2ull * ((n_buckets + kScanBlock - 1) / kScanBlock) + 2;
+}
+
+cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st, cudaEvent_t *ev) {
+  cudaError_t e;
+  auto mark = [&](int k) {
+    if (ev) cudaEventRecord(ev[k], st);
+  };
+  if ((e = cudaMemsetAsync(pb.count, 0, (size_t)pb.n_buckets * 4, st))) return e;
+  if ((e = cudaMemsetAsync(pb.fill, 0, (size_t)pb.n_buckets * 4, st))) return e;
+  if ((e = cudaMemsetAsync(pb.counters, 0, CNT_WORDS * 4, st))) return e;
+  mark(0);
+  const uint32_t pts_blocks = (uint32_t)((pb.n_points + 255) / 256);
+  if (pb.n_points > 0) k_count<<<pts_blocks, 256, 0, st>>>(pb);
+  mark(1);
+  const uint32_t nblk = (pb.n_buckets + kScanBlock - 1) / kScanBlock;
+  if (nblk > 0) {
+    k_scan_reduce<<<nblk, kScanThreads, 0, st>>>(pb);
+    k_scan_blocks<<<1, kScanThreads, 0, st>>>(pb, nblk);
+    k_scan_apply<<<nblk, kScanThreads, 0, st>>>(pb);
+  }
+  mark(2);
+  if (pb.n_points > 0) k_scatter<<<pts_blocks, 256, 0, st>>>(pb);
+  mark(3);
+  if (pb.n_buckets > 0) k_tasks<<<(pb.n_buckets + 255) / 256, 256, 0, st>>>(pb);
+  mark(4);
+  k_accumulate<<<num_sms * 2, 256, 0, st>>>(pb);
+  mark(5);
+  k_merge<<<num_sms, 256, 0, st>>>(pb);
+  mark(6);
+  if (pb.n_segs > 0) k_reduce1<<<(pb.n_segs + 127) / 128, 128, 0, st>>>(pb);
+  mark(7);
+  if (pb.n_wins > 0) k_reduce2<<<pb.n_wins, kRed2Threads, 0, st>>>(pb);
+  mark(8);
+  if (pb.n_jobs > 0) k_final<<<pb.n_jobs, 128, 0, st>>>(pb);
+  mark(9);
+  return cudaGetLastError();
+}

@@ -1,0 +1,161 @@
+/* GB300 multi-scalar multiplication engine for BLS12-377 G1 -- C ABI of libdriver.so.
+ *
+ * The first two entry points are a drop-in for the host driver of fyquah/hardcaml_zprize's MSM
+ * track: same symbol names, same argument meaning, same struct layout, so the reference's Rust
+ * harness (zprize/msm_pippenger/test_fpga_harness/src/lib.rs:18-33, linked with
+ * `cargo:rustc-link-lib=dylib=driver`, build.rs:19) binds them unchanged.
+ *
+ * Data layout (zprize/msm_pippenger/host/msm_compute/include/bls12_377_g1/rust_types.h:8-83):
+ *   - base-field elements are six little-endian u64 limbs in arkworks Montgomery form
+ *     (value * 2^384 mod q), fully reduced;
+ *   - scalars are four little-endian u64 limbs, the raw integer the harness transmutes out of
+ *     ark_bls12_377::Fr (tests/msm.rs:30-32); bits 253..255 are ignored, as the reference's
+ *     253-bit scalar path does (driver.cpp:15, bls12_377_g1.h:17);
+ *   - results are arkworks 0.3 Jacobian projective points: (x*R, y*R, R) for a finite point,
+ *     (R, R, 0) for the point at infinity (the reference writes (x*R, y*R, R) too,
+ *     bls12_377_g1.h:427-439, 667-690).
+ */
+#ifndef MSM_GB300_H
+#define MSM_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <sys/types.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  uint64_t data[4];
+} biginteger256_t; /* 32 B, rust_types.h:8-63 */
+
+typedef struct {
+  uint64_t data[6];
+} biginteger384_t; /* 48 B, rust_types.h:65-71 */
+
+typedef struct {
+  biginteger384_t x;
+  biginteger384_t y;
+  bool infinity;
+} g1_affine_t; /* 104 B with padding, rust_types.h:73-77 (arkworks GroupAffine) */
+
+typedef struct {
+  biginteger384_t x;
+  biginteger384_t y;
+  biginteger384_t z;
+} g1_projective_t; /* 144 B, rust_types.h:79-83 (arkworks GroupProjective, Jacobian) */
+
+/* ---------------------------------------------------------------------------------------------
+ * Drop-in entry points
+ * ------------------------------------------------------------------------------------------- */
+
+/* Load the bases once and keep them resident on the GPU in precomputed twisted-Edwards form.
+ * Replaces `extern "C" Driver *msm_init(const char *xclbin, ssize_t xclbin_len,
+ * g1_affine_t *rust_points, ssize_t npoints)` (zprize/msm_pippenger/host/driver/driver.cpp:603-617).
+ * `xclbin` names an FPGA bitstream in the reference; here it is accepted and ignored (it may be
+ * NULL). `points` is borrowed for the call. Returns NULL on failure (msm_last_error() says why);
+ * the reference exits the process instead (driver.cpp:248-251). */
+void *msm_init(const char *xclbin, ssize_t xclbin_len, const g1_affine_t *points, ssize_t npoints);
+
+/* Run `batch_size` MSMs over all resident bases: out[b] = sum_i scalars[b*npoints + i] * P_i.
+ * Replaces `extern "C" void msm_mult(Driver *driver, g1_projective_t *out, uint64_t num_batches,
+ * biginteger256_t *ptr_scalars)` (driver.cpp:619-636). `out` holds batch_size results (caller
+ * allocated, as lib.rs:70 does). On failure every output is zeroed and msm_last_error() is set. */
+void msm_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+              const biginteger256_t *scalars);
+
+/* ---------------------------------------------------------------------------------------------
+ * Additions (no counterpart in the reference unless stated)
+ * ------------------------------------------------------------------------------------------- */
+
+/* Tuning knobs; 0 (or a negative value) means "choose automatically". */
+typedef struct {
+  int32_t window_bits;   /* c, 6..22 */
+  int32_t signed_digits; /* 1 signed c-bit digits, 2 unsigned digits, 0 auto (signed) */
+  int32_t seg_len;       /* max entries one thread accumulates before a bucket is split */
+  int32_t red_len_log2;  /* log2 of buckets per level-1 reduction segment */
+  int32_t use_graph;     /* 1 replay the pass from a captured CUDA graph, 2 never, 0 auto */
+  int32_t mode;          /* msm_mult: 1 one pass per MSM (default), 2 all MSMs in one pass */
+} msm_options_t;
+
+/* Error code of the last failed call on this thread (0 if none) and its message. */
+int msm_last_error(char *buf, size_t len);
+
+/* Release a context (the reference never frees its Driver). */
+void msm_free(void *context);
+
+/* msm_mult with explicit options; returns 0 or a negative error code. */
+int msm_mult_ex(void *context, g1_projective_t *out, uint64_t batch_size,
+                const biginteger256_t *scalars, const msm_options_t *opt);
+
+/* Many MSMs of uneven sizes in one pass with one shared sort. MSM j uses sizes[j] bases starting
+ * at base_offsets[j] and the next sizes[j] scalars of the concatenated `scalars` array.
+ * opt->mode == 1 runs them one pass per MSM instead (the plain form). */
+int msm_mult_uneven(void *context, g1_projective_t *out, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const biginteger256_t *scalars,
+                    const msm_options_t *opt);
+
+/* As msm_mult_uneven, with the scalars already in device memory (`d_scalars`, 32 B each);
+ * results are written to host memory. */
+int msm_mult_device(void *context, g1_projective_t *out, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const void *d_scalars, const msm_options_t *opt);
+
+/* The configuration the engine would use for one MSM of `npoints` (after tuning, if any). */
+int msm_get_config(void *context, uint64_t npoints, msm_options_t *out);
+
+/* Measure candidate configurations for MSMs of `npoints` on the device and keep the fastest for
+ * that size class (persisted to the file named by MSM_TUNE_CACHE, if set). `budget_ms` bounds
+ * the time spent (0: default). Returns 0 and fills `best` (may be NULL). */
+int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *best);
+
+/* Per-stage device times (ms, CUDA events on the pipeline stream) of the last pass when timing
+ * is enabled with msm_set_timing(ctx, 1). Stage order: count, scan, scatter, tasks, accumulate,
+ * merge, reduce1, reduce2, final. Returns the number of stages written. */
+int msm_set_timing(void *context, int32_t enable);
+int msm_last_timings(void *context, double *ms, int32_t max_stages);
+/* Counters of the last pass: tasks, heavy buckets, sorted entries, buckets. */
+int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats);
+
+/* ---- serving: continuous batching of MSM requests against the resident bases ---- */
+typedef struct {
+  uint64_t submitted, completed, passes, inflight_peak;
+  uint64_t bytes_in_use, bytes_peak;
+} msm_server_stats_t;
+
+/* `hbm_budget_bytes` bounds the device memory of scalar/sort/bucket buffers of passes in
+ * flight; `max_inflight` bounds concurrent passes (each on its own stream). */
+void *msm_server_create(void *context, uint64_t hbm_budget_bytes, int32_t max_inflight);
+/* Copy the request's scalars and queue it; returns its id (>= 0) or a negative error. */
+int64_t msm_server_submit(void *server, const biginteger256_t *scalars, uint64_t n,
+                          uint64_t base_offset);
+/* 0 done (result in *out, latency from submit to completion in *latency_ms if not NULL),
+ * 1 still pending after waiting up to wait_ms, negative on error. */
+int msm_server_poll(void *server, int64_t id, g1_projective_t *out, int32_t wait_ms,
+                    double *latency_ms);
+int msm_server_stats(void *server, msm_server_stats_t *stats);
+void msm_server_destroy(void *server);
+
+/* ---- utilities for tests and benchmarks ---- */
+/* Bases k_i * G, k_i a seeded counter-based 64-bit draw (SplitMix64), computed on the GPU. */
+int msm_generate_bases(uint64_t seed, uint64_t first, uint64_t n, g1_affine_t *out);
+/* Scalars on the host: kind 0 uniform in [0, r); kind 1 the uneven-batch mix (70% uniform,
+ * 10% 16-bit, 10% 0 or r-1, 10% one repeated value), drawn for MSM `msm_index`. */
+int msm_generate_scalars(uint64_t seed, uint64_t n, int32_t kind, uint64_t msm_index,
+                         biginteger256_t *out);
+/* Measured peak rate of the GPU's IMAD pipe (32-bit multiply-adds per second, all SMs). */
+double msm_measure_imad_peak(int32_t iters);
+/* Device name, SM count and clock as text. */
+int msm_device_info(char *buf, size_t len);
+/* Field self-test: op 0 mul (Montgomery), 1 add, 2 sub, 3 inverse, 4 canonicalise, 5 negate;
+ * operands are 12 little-endian u32 limbs each. */
+int msm_field_selftest(int32_t op, const uint32_t *a, const uint32_t *b, uint32_t *out, uint64_t n);
+/* Throughput of the mixed twisted-Edwards addition on cached bases (adds per second). */
+double msm_measure_madd_rate(void *context, int32_t iters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSM_GB300_H */

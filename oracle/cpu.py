@@ -1,0 +1,66 @@
+"""ctypes bridge to the C oracle (oracle/cpu_msm.c) -- test infrastructure only.
+
+Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker and the
+timed CPU baseline; the GPU engine never calls it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        path = mod.build()
+        L = ctypes.CDLL(path)
+        P, U64, I = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+        L.oracle_msm.argtypes = [P, P, U64, I, I, P]
+        L.oracle_msm.restype = I
+        L.oracle_gen_bases.argtypes = [U64, U64, U64, P, I]
+        L.oracle_gen_bases.restype = I
+        L.oracle_mul.argtypes = [P, P, P]
+        L.oracle_mul.restype = I
+        L.oracle_default_window.argtypes = [U64]
+        L.oracle_default_window.restype = I
+        L.oracle_rand_u64.argtypes = [U64, U64, U64, U64]
+        L.oracle_rand_u64.restype = U64
+        _lib = L
+    return _lib
+
+
+def msm(points: np.ndarray, scalars: np.ndarray, c: int = 0, threads: int = 0) -> np.ndarray:
+    """One MSM: points (n, 104) uint8, scalars (n, 4) uint64 -> (144,) uint8 g1_projective_t."""
+    pts = np.ascontiguousarray(points, dtype=np.uint8).reshape(-1, 104)
+    sc = np.ascontiguousarray(scalars, dtype=np.uint64).reshape(-1, 4)
+    assert pts.shape[0] == sc.shape[0]
+    out = np.zeros(144, dtype=np.uint8)
+    lib().oracle_msm(pts.ctypes.data, sc.ctypes.data, pts.shape[0], c, threads, out.ctypes.data)
+    return out
+
+
+def gen_bases(seed: int, n: int, first: int = 0, threads: int = 0) -> np.ndarray:
+    out = np.zeros((n, 104), dtype=np.uint8)
+    lib().oracle_gen_bases(seed, first, n, out.ctypes.data, threads)
+    return out
+
+
+def mul(point: np.ndarray, k: int) -> np.ndarray:
+    p = np.ascontiguousarray(point, dtype=np.uint8).reshape(104)
+    kk = np.array([(k >> (64 * i)) & (2**64 - 1) for i in range(4)], dtype=np.uint64)
+    out = np.zeros(144, dtype=np.uint8)
+    lib().oracle_mul(p.ctypes.data, kk.ctypes.data, out.ctypes.data)
+    return out
+
+
+def default_window(n: int) -> int:
+    return lib().oracle_default_window(n)

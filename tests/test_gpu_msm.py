@@ -1,0 +1,301 @@
+"""Parity of the GPU engine (through the C ABI) with the oracle.
+
+Every comparison is bit-exact: both sides write results as (x*R, y*R, R) or (R, R, 0) with
+canonical limbs, so the 144-byte records must be identical; the Python oracle additionally checks
+the canonical affine point, which is what the reference harness compares
+(test_fpga_harness/tests/msm.rs:35-40).
+"""
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+Q = None
+
+
+def recs(ref, pts):
+    return np.frombuffer(b"".join(ref.encode_affine(p) for p in pts), dtype=np.uint8).reshape(-1, 104).copy()
+
+
+def scal(ref, ks):
+    return np.frombuffer(b"".join(ref.encode_scalar(k) for k in ks), dtype=np.uint64).reshape(-1, 4).copy()
+
+
+def msm_gpu(engine, points, scalars, **opts):
+    ctx = engine.multi_scalar_mult_init(points)
+    try:
+        if opts:
+            return ctx.mult(scalars, **opts)
+        return engine.multi_scalar_mult(ctx, points, scalars)
+    finally:
+        ctx.close()
+
+
+# ---- field arithmetic ----------------------------------------------------------------------
+def limbs32(v, n=12):
+    return [(v >> (32 * i)) & 0xFFFFFFFF for i in range(n)]
+
+
+def from32(a):
+    return sum(int(x) << (32 * i) for i, x in enumerate(a))
+
+
+def test_field_ops(engine, ref):
+    Q = ref.Q
+    R = 2**384
+    rng = random.Random(1)
+    vals = [0, 1, 2, Q - 1, Q, Q + 1, 2 * Q - 1, ref.MONT_R, (R - 1) % (2 * Q)]
+    vals += [rng.randrange(2 * Q) for _ in range(500)]
+    other = [rng.randrange(2 * Q) for _ in vals]
+    a = np.array([limbs32(v) for v in vals], dtype=np.uint32)
+    b = np.array([limbs32(v) for v in other], dtype=np.uint32)
+    Rinv = pow(R, -1, Q)
+    mul = engine.field_selftest(0, a, b)
+    add = engine.field_selftest(1, a, b)
+    sub = engine.field_selftest(2, a, b)
+    can = engine.field_selftest(4, a, b)
+    neg = engine.field_selftest(5, a, b)
+    inv = engine.field_selftest(3, a, b)
+    for i, (x, y) in enumerate(zip(vals, other)):
+        m = from32(mul[i])
+        assert m < 2 * Q and m % Q == x * y * Rinv % Q
+        s = from32(add[i])
+        assert s < 2 * Q and s % Q == (x + y) % Q
+        d = from32(sub[i])
+        assert d < 2 * Q and d % Q == (x - y) % Q
+        c = from32(can[i])
+        assert c < Q and c == x % Q
+        ng = from32(neg[i])
+        assert ng < 2 * Q and ng % Q == (-x) % Q
+        iv = from32(inv[i])
+        if x % Q:
+            assert iv % Q * x % Q == R * R % Q
+        else:
+            assert iv % Q == 0
+
+
+# ---- generator -------------------------------------------------------------------------------
+def test_generated_bases_match_oracle(engine, ocpu):
+    got = engine.generate_bases(99, 300)
+    assert np.array_equal(got, ocpu.gen_bases(99, 300))
+    got = engine.generate_bases(99, 64, first=1 << 20)
+    assert np.array_equal(got, ocpu.gen_bases(99, 64, first=1 << 20))
+
+
+# ---- MSM parity -------------------------------------------------------------------------------
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 64, 1000])
+def test_msm_small(engine, ref, ocpu, n):
+    pts = ocpu.gen_bases(7 + n, n)
+    sc = engine.generate_scalars(11 + n, 2 * n)
+    out = msm_gpu(engine, pts, sc)
+    for b in range(2):
+        want = ocpu.msm(pts, sc[b * n:(b + 1) * n])
+        assert np.array_equal(out[b], want), f"batch {b}"
+
+
+def test_msm_config_2_12(engine, ocpu):
+    """Plain single MSM, N = 2^12, seeded bases k_i * G and uniform scalars (4 batches)."""
+    n = 1 << 12
+    pts = ocpu.gen_bases(2024, n)
+    sc = engine.generate_scalars(2025, 4 * n)
+    out = msm_gpu(engine, pts, sc)
+    for b in range(4):
+        assert np.array_equal(out[b], ocpu.msm(pts, sc[b * n:(b + 1) * n]))
+
+
+@pytest.mark.parametrize("opts", [
+    dict(window_bits=6), dict(window_bits=8), dict(window_bits=11), dict(window_bits=13),
+    dict(window_bits=16), dict(window_bits=9, signed_digits=2), dict(window_bits=12, signed_digits=2),
+    dict(window_bits=10, seg_len=3), dict(window_bits=7, seg_len=1, red_len_log2=2),
+    dict(mode=2), dict(mode=2, use_graph=1), dict(use_graph=1),
+])
+def test_msm_knobs(engine, ocpu, opts):
+    n = 1500
+    pts = ocpu.gen_bases(31, n)
+    sc = engine.generate_scalars(32, 2 * n)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        for rep in range(2):
+            out = ctx.mult(sc, **opts)
+            for b in range(2):
+                assert np.array_equal(out[b], ocpu.msm(pts, sc[b * n:(b + 1) * n])), (opts, rep, b)
+    finally:
+        ctx.close()
+
+
+def test_trivial_inputs(engine, ref, ocpu):
+    """TEST_TRIVIAL_INPUTS of the harness (util.rs:164-183): all bases G, scalar[0] = 1."""
+    n = 256
+    pts = recs(ref, [ref.GEN] * n)
+    sc = np.zeros((4 * n, 4), dtype=np.uint64)
+    sc[::n, 0] = 1
+    out = msm_gpu(engine, pts, sc)
+    for b in range(4):
+        assert ref.decode_projective(out[b].tobytes()) == ref.GEN
+
+
+def test_edge_scalars_and_bases(engine, ref, ocpu):
+    rng = random.Random(5)
+    n = 777
+    pts = [ref.mul(ref.GEN, rng.getrandbits(64)) for _ in range(40)]
+    plist = [pts[i % 40] for i in range(n)]
+    plist[3] = ref.INF
+    plist[100] = ref.INF
+    ks = [rng.randrange(ref.R_SCALAR) for _ in range(n)]
+    for i in range(0, n, 7):
+        ks[i] = 0
+    for i in range(1, n, 11):
+        ks[i] = ref.R_SCALAR - 1
+    for i in range(2, n, 5):
+        ks[i] = 0xABCDEF  # one heavy bucket per low window
+    ks[5] = (1 << 253) - 1
+    ks[6] = ks[7] | (5 << 253)  # bits above 253 are ignored
+    P, S = recs(ref, plist), scal(ref, ks)
+    out = msm_gpu(engine, P, S)
+    assert np.array_equal(out[0], ocpu.msm(P, S))
+    for opts in (dict(window_bits=8, seg_len=4), dict(window_bits=16)):
+        assert np.array_equal(msm_gpu(engine, P, S, **opts)[0], ocpu.msm(P, S))
+
+
+def test_all_scalars_zero_and_empty(engine, ref, ocpu):
+    pts = ocpu.gen_bases(3, 50)
+    out = msm_gpu(engine, pts, np.zeros((50, 4), dtype=np.uint64))
+    assert ref.decode_projective(out[0].tobytes()) is ref.INF
+    assert np.array_equal(out[0], ocpu.msm(pts, np.zeros((50, 4), dtype=np.uint64)))
+
+
+# ---- the reference harness's five edge-case tests (tests/msm_unit_tests.rs) ------------------
+def special_points(ref, kats):
+    return [ref.parse_hex_point(p["x"], p["y"]) for p in kats["non_te_points"]]
+
+
+def check_case(engine, ref, ocpu, pts, ks, batches=1):
+    P = recs(ref, pts)
+    S = scal(ref, ks)
+    out = msm_gpu(engine, P, S)
+    n = len(pts)
+    for b in range(batches):
+        want = ref.msm_naive(pts, ks[b * n:(b + 1) * n])
+        assert ref.decode_projective(out[b].tobytes()) == want
+        assert np.array_equal(out[b], ocpu.msm(P, S[b * n:(b + 1) * n]))
+
+
+def test_intermediate_infinity_non_representable_1(engine, ref, ocpu, kats):
+    sp = special_points(ref, kats)  # msm_unit_tests.rs:19-77
+    check_case(engine, ref, ocpu, [sp[0], sp[1], sp[2], sp[2]], [1, 1, 1, 1])
+
+
+def test_intermediate_infinity_non_representable_2(engine, ref, ocpu, kats):
+    sp = special_points(ref, kats)  # msm_unit_tests.rs:81-133
+    pts = [sp[0], sp[2], ref.neg(ref.add(sp[0], sp[2])), sp[2]]
+    check_case(engine, ref, ocpu, pts, [1, 1, 1, 1])
+
+
+def test_infinity_result(engine, ref, ocpu):
+    pts = [ref.GEN if i % 2 == 0 else ref.neg(ref.GEN) for i in range(256)]  # :137-180
+    check_case(engine, ref, ocpu, pts, [1] * (4 * 256), batches=4)
+
+
+def test_unrepresentable_points_at_chunk_boundaries(engine, ref, ocpu, kats):
+    sp = special_points(ref, kats)  # :185-240
+    n = 1 << 12
+    P = ocpu.gen_bases(4242, n)
+    for idx, p in ((1024, sp[0]), (2047, sp[2]), (3 * 1024 - 1, sp[1]), (4095, sp[2])):
+        P[idx] = np.frombuffer(ref.encode_affine(p), dtype=np.uint8)
+    S = engine.generate_scalars(4243, 4 * n)
+    out = msm_gpu(engine, P, S)
+    for b in range(4):
+        assert np.array_equal(out[b], ocpu.msm(P, S[b * n:(b + 1) * n]))
+
+
+def test_one_unrepresentable_one_regular(engine, ref, ocpu, kats):
+    sp = special_points(ref, kats)  # :244-290
+    check_case(engine, ref, ocpu, [ref.GEN, sp[0]], [1, 2])
+
+
+def test_rtl_bucket_kat_through_engine(engine, ref, kats):
+    """The single-point case of test_top.ml:148-193 (scalar 82 on a k*G base) end to end."""
+    kat = kats["rtl_bucket_kat"]
+    px = int(next(e for e in kat["entries"] if e["point"])["point"]["x"], 16)
+    k = next(k for k in range(1, 100) if ref.mul(ref.GEN, k)[0] == px)
+    P = ref.mul(ref.GEN, k)
+    out = msm_gpu(engine, recs(ref, [P]), scal(ref, [82]))
+    assert ref.decode_projective(out[0].tobytes()) == ref.mul(P, 82)
+
+
+# ---- uneven batches, graphs, server, tuner ----------------------------------------------------
+def test_uneven_batch_modes(engine, ocpu):
+    nb = 1 << 12
+    pts = ocpu.gen_bases(77, nb)
+    rng = random.Random(9)
+    sizes = [1, 0, 5, 64, 1000, 4096, 333, 2048, 17, 4000, 1, 999]
+    offs = [rng.randrange(0, nb - s + 1) for s in sizes]
+    sc = np.concatenate([engine.generate_scalars(500, s, kind=1, msm_index=j) for j, s in enumerate(sizes)])
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        first = np.concatenate([[0], np.cumsum(sizes)])
+        want = [ocpu.msm(pts[o:o + s], sc[first[j]:first[j] + s]) for j, (s, o) in enumerate(zip(sizes, offs))]
+        for opts in (dict(mode=1), dict(mode=2), dict(mode=2, use_graph=1), dict(mode=2, use_graph=2)):
+            for rep in range(2):
+                out = ctx.mult_uneven(sizes, offs, sc, **opts)
+                for j in range(len(sizes)):
+                    assert np.array_equal(out[j], want[j]), (opts, rep, j)
+    finally:
+        ctx.close()
+
+
+def test_server_results_alone_and_in_the_mix(engine, ocpu):
+    nb = 1 << 12
+    pts = ocpu.gen_bases(8, nb)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        sizes = [4096, 100, 2000, 1, 3000, 512, 4096, 50]
+        offs = [0, 17, 1000, 4095, 500, 3000, 0, 4000]
+        reqs = [engine.generate_scalars(600 + j, s) for j, s in enumerate(sizes)]
+        alone = [ctx.mult_uneven([s], [o], r)[0] for s, o, r in zip(sizes, offs, reqs)]
+        srv = engine.MsmServer(ctx, hbm_budget_bytes=64 << 20, max_inflight=2)
+        try:
+            ids = [srv.submit(r, o) for r, o in zip(reqs, offs)]
+            for j, rid in enumerate(ids):
+                res = srv.poll(rid, wait_ms=60000)
+                assert res is not None
+                out, lat = res
+                assert lat >= 0
+                assert np.array_equal(out, alone[j])
+                assert np.array_equal(out, ocpu.msm(pts[offs[j]:offs[j] + sizes[j]], reqs[j]))
+            st = srv.stats()
+            assert st["completed"] == len(sizes) and st["passes"] >= 1
+        finally:
+            srv.close()
+        with pytest.raises(engine.MsmError):
+            small = engine.MsmServer(ctx, hbm_budget_bytes=1 << 10, max_inflight=1)
+            try:
+                small.submit(reqs[0], 0)
+            finally:
+                small.close()
+    finally:
+        ctx.close()
+
+
+def test_tuner_keeps_results_exact(engine, ocpu):
+    n = 1 << 12
+    pts = ocpu.gen_bases(55, n)
+    sc = engine.generate_scalars(56, n)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        best = ctx.tune(n, budget_ms=5000)
+        assert 6 <= best["window_bits"] <= 21
+        assert ctx.config(n)["window_bits"] == best["window_bits"]
+        assert np.array_equal(ctx.mult(sc)[0], ocpu.msm(pts, sc))
+    finally:
+        ctx.close()
+
+
+def test_msm_2_18_against_oracle(engine, ocpu):
+    n = 1 << 18
+    pts = engine.generate_bases(1, n)
+    sc = engine.generate_scalars(2, n)
+    out = msm_gpu(engine, pts, sc)
+    assert np.array_equal(out[0], ocpu.msm(pts, sc))
