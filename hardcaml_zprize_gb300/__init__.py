@@ -36,6 +36,7 @@ EXPORTED = [
     "msm_last_pass_stats", "msm_server_create", "msm_server_submit", "msm_server_poll",
     "msm_server_stats", "msm_server_destroy", "msm_generate_bases", "msm_generate_scalars",
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
+    "msm_mult_noalloc",
 ]
 
 STAGES = ["count", "scan", "scatter", "tasks", "accumulate", "merge", "reduce1", "reduce2", "final"]
@@ -93,6 +94,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "msm_device_info": (ctypes.c_int, [ctypes.c_char_p, SZ]),
         "msm_field_selftest": (ctypes.c_int, [I32, P, P, P, U64]),
         "msm_measure_madd_rate": (ctypes.c_double, [P, I32]),
+        "msm_mult_noalloc": (ctypes.c_int, [P, P, U64, U64, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -217,6 +219,15 @@ class MultiScalarMultContext:
         arr = (ctypes.c_uint64 * 4)()
         load_library().msm_last_pass_stats(self.handle, arr, 4)
         return {"tasks": arr[0], "heavy_buckets": arr[1], "max_entries": arr[2], "buckets": arr[3]}
+
+    def mult_noalloc(self, n: int, base_offset: int, d_scalars_ptr: int, d_out_ptr: int,
+                     stream: int = 0) -> None:
+        """Enqueue one MSM of n <= 65536 points that allocates no device memory: the caller
+        passes device pointers for the scalars and the 144-byte result and synchronises."""
+        _check(load_library().msm_mult_noalloc(self.handle, ctypes.c_void_p(d_out_ptr), n,
+                                               base_offset, ctypes.c_void_p(d_scalars_ptr),
+                                               ctypes.c_void_p(stream) if stream else None),
+               "msm_mult_noalloc")
 
     def madd_rate(self, iters: int = 2000) -> float:
         return load_library().msm_measure_madd_rate(self.handle, iters)

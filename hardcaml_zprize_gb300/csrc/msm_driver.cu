@@ -1316,3 +1316,156 @@ int msm_field_selftest(int32_t op, const uint32_t *a, const uint32_t *b, uint32_
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// msm_mult_noalloc: one MSM whose scratch lives in a fixed, file-scope device array.
+//
+// Some callers cannot allocate device memory at call time.  Examples: a plugin that runs inside
+// another runtime's memory pool, a request loop that must not stall, and a host callback that
+// may not call CUDA allocation functions.  cudaMalloc and cudaFree synchronise the device, and
+// an allocation can fail halfway through a request.  This entry point uses only memory that
+// exists before the call: the context's resident bases (allocated once by msm_init), the
+// caller's scalars and output, and the array below for every intermediate buffer.
+//
+// The array takes MSM_NOALLOC_SCRATCH_BYTES (24 MiB) on every GPU that loads the library, until
+// the process exits.  Every call shares it and it keeps the last call's contents.  The pipeline
+// clears its own counters at the start of each call, so nothing leaks from one call into the
+// next.  Calls that overlap on the GPU (different streams, or other threads) race on the array;
+// callers must order them, for example by issuing them on one stream.
+// =============================================================================================
+#define MSM_NOALLOC_MAX_POINTS (1u << 16)
+#define MSM_NOALLOC_SCRATCH_BYTES (24u << 20)
+#define MSM_NOALLOC_WINDOW_BITS 12u
+#define MSM_NOALLOC_SEG_LEN 256u
+#define MSM_NOALLOC_RED_LOG2 3u
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[MSM_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[256] = {};  // device address of g_noalloc_scratch, per device ordinal
+
+// window descriptors of the single MSM, written on the device so no host staging is needed
+__global__ void k_noalloc_plan(JobDesc jd, uint32_t red_log2, JobDesc *jobs, WinDesc *wins) {
+  const uint32_t w = threadIdx.x;
+  if (w == 0) jobs[0] = jd;
+  if (w >= jd.nwin) return;
+  const uint32_t L = 1u << red_log2;
+  const uint32_t nseg_low = (jd.nb + L - 1) / L;
+  WinDesc wd;
+  wd.job = 0;
+  wd.w = w;
+  wd.bucket_begin = jd.bucket_begin + w * jd.nb;
+  wd.nb = (w + 1 == jd.nwin) ? jd.nb_top : jd.nb;
+  wd.seg_begin = w * nseg_low;
+  wd.nseg = (wd.nb + L - 1) / L;
+  wins[w] = wd;
+}
+
+size_t carve(size_t &off, size_t bytes) {
+  const size_t at = off;
+  off += (bytes + 255) & ~(size_t)255;
+  return at;
+}
+
+}  // namespace
+
+extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t n,
+                                uint64_t base_offset, const biginteger256_t *d_scalars,
+                                void *stream) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || !d_out || (n && !d_scalars)) return fail(ERR_ARG, "msm_mult_noalloc: null argument");
+  if (n > MSM_NOALLOC_MAX_POINTS)
+    return fail(ERR_BUDGET, "msm_mult_noalloc: %llu points is over the maximum of %u",
+                (unsigned long long)n, MSM_NOALLOC_MAX_POINTS);
+  if (base_offset > cx->npoints || n > cx->npoints - base_offset)
+    return fail(ERR_ARG, "msm_mult_noalloc: bases outside the resident set");
+  CK(cudaSetDevice(cx->device));
+  void *scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (cx->device < 0 || cx->device >= 256) return fail(ERR_DEVICE, "device ordinal out of range");
+    if (!g_noalloc_ptr[cx->device]) {
+      void *p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return fail(ERR_CUDA, "msm_mult_noalloc: cudaGetSymbolAddress failed: %s",
+                    cudaGetErrorString(e));
+      g_noalloc_ptr[cx->device] = p;
+    }
+    scratch = g_noalloc_ptr[cx->device];
+  }
+  // fixed layout: c = 12 signed windows (22 windows, 2048 buckets each, 2 in the top window)
+  JobDesc jd{};
+  jd.n = n;
+  jd.base_off = base_offset;
+  jd.c = MSM_NOALLOC_WINDOW_BITS;
+  jd.signed_digits = 1;
+  uint32_t nbk = 0, nsegs = 0;
+  const uint32_t L = 1u << MSM_NOALLOC_RED_LOG2;
+  if (n) {
+    layout(jd.c, 1, jd.nwin, jd.nb, jd.nb_top);
+    nbk = (jd.nwin - 1) * jd.nb + jd.nb_top;
+    nsegs = (jd.nwin - 1) * ((jd.nb + L - 1) / L) + (jd.nb_top + L - 1) / L;
+  }
+  const uint64_t entries = n * jd.nwin;
+  const uint32_t tasks = (uint32_t)(nbk + entries / MSM_NOALLOC_SEG_LEN + 1);
+  size_t off = 0;
+  const size_t o_jobs = carve(off, sizeof(JobDesc));
+  const size_t o_wins = carve(off, 64 * sizeof(WinDesc));
+  const size_t o_count = carve(off, (size_t)nbk * 4), o_offset = carve(off, (size_t)nbk * 4);
+  const size_t o_fill = carve(off, (size_t)nbk * 4), o_taskoff = carve(off, (size_t)nbk * 4);
+  const size_t o_heavy = carve(off, (size_t)nbk * 4);
+  const size_t o_scan = carve(off, msm_scan_tmp_words(nbk) * 4);
+  const size_t o_cnt = carve(off, CNT_WORDS * 4);
+  const size_t o_vals = carve(off, entries * 4);
+  const size_t o_tasks = carve(off, (size_t)tasks * sizeof(Task));
+  const size_t o_part = carve(off, (size_t)tasks * MSM_BUCKET_BYTES);
+  const size_t o_seg = carve(off, (size_t)nsegs * 2 * MSM_BUCKET_BYTES);
+  const size_t o_win = carve(off, (size_t)jd.nwin * MSM_BUCKET_BYTES);
+  if (off > MSM_NOALLOC_SCRATCH_BYTES)
+    return fail(ERR_BUDGET, "msm_mult_noalloc: scratch layout needs %zu bytes", off);
+  uint8_t *s = (uint8_t *)scratch;
+  PassBuffers pb{};
+  pb.bases = cx->bases.as<uint4>();
+  pb.flags = cx->flags.as<uint8_t>();
+  pb.special_idx = cx->special_idx.as<uint32_t>();
+  pb.special_cls = cx->special_cls.as<uint8_t>();
+  pb.class_pts = cx->class_pts.as<uint4>();
+  pb.n_special = cx->n_special;
+  pb.n_classes = cx->n_classes;
+  pb.n_bases = cx->npoints;
+  pb.scalars = (const uint4 *)d_scalars;
+  pb.jobs = (const JobDesc *)(s + o_jobs);
+  pb.wins = (const WinDesc *)(s + o_wins);
+  pb.n_jobs = 1;
+  pb.n_wins = jd.nwin;
+  pb.n_points = n;
+  pb.n_buckets = nbk;
+  pb.n_segs = nsegs;
+  pb.seg_len = MSM_NOALLOC_SEG_LEN;
+  pb.red_len_log2 = MSM_NOALLOC_RED_LOG2;
+  pb.max_entries = entries;
+  pb.max_tasks = tasks;
+  pb.count = (uint32_t *)(s + o_count);
+  pb.offset = (uint32_t *)(s + o_offset);
+  pb.fill = (uint32_t *)(s + o_fill);
+  pb.taskoff = (uint32_t *)(s + o_taskoff);
+  pb.heavy = (uint32_t *)(s + o_heavy);
+  pb.scan_tmp = (uint32_t *)(s + o_scan);
+  pb.counters = (uint32_t *)(s + o_cnt);
+  pb.vals = (uint32_t *)(s + o_vals);
+  pb.tasks = (Task *)(s + o_tasks);
+  pb.partials = (uint4 *)(s + o_part);
+  pb.seg_out = (uint4 *)(s + o_seg);
+  pb.win_sum = (uint4 *)(s + o_win);
+  pb.results = (uint64_t *)d_out;
+  cudaStream_t st = (cudaStream_t)stream;
+  k_noalloc_plan<<<1, 64, 0, st>>>(jd, MSM_NOALLOC_RED_LOG2, (JobDesc *)(s + o_jobs),
+                                   (WinDesc *)(s + o_wins));
+  CK(cudaGetLastError());
+  CK(msm_launch_pass(pb, cx->num_sms, st, nullptr));
+  return 0;
+}

@@ -118,6 +118,21 @@ int msm_last_timings(void *context, double *ms, int32_t max_stages);
 /* Counters of the last pass: tasks, heavy buckets, sorted entries, buckets. */
 int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats);
 
+/* One MSM that allocates no device memory; it has no counterpart in the reference.
+ * For callers that cannot call cudaMalloc at call time: a plugin running inside another
+ * runtime's memory pool, a request loop that must not stall, a host callback that may not
+ * allocate (cudaMalloc/cudaFree synchronise the device and can fail mid-request).
+ * Inputs and output are the caller's device memory: `d_scalars` (n x 32 B) and `d_out`
+ * (one g1_projective_t); the bases are the context's resident slice [base_offset,
+ * base_offset + n).  Intermediate buffers live in one file-scope device array of 24 MiB that
+ * every GPU loading the library holds until the process exits; n may be at most 65536 (larger n
+ * is rejected with an error).  The first call on a device looks up that array's address, so
+ * make the first call before any stream capture.  The call only enqueues work on `stream`
+ * (NULL: the legacy default stream); synchronise it before reading `d_out`.  All calls share
+ * the array: calls that overlap on the GPU race, so order them (for example on one stream). */
+int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t n, uint64_t base_offset,
+                     const biginteger256_t *d_scalars, void *stream);
+
 /* ---- serving: continuous batching of MSM requests against the resident bases ---- */
 typedef struct {
   uint64_t submitted, completed, passes, inflight_peak;
