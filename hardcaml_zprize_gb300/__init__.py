@@ -36,16 +36,18 @@ EXPORTED = [
     "msm_last_pass_stats", "msm_server_create", "msm_server_submit", "msm_server_poll",
     "msm_server_stats", "msm_server_destroy", "msm_generate_bases", "msm_generate_scalars",
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
-    "msm_mult_noalloc",
+    "msm_mult_noalloc", "msm_measure_int_peaks",
 ]
 
-STAGES = ["count", "scan", "scatter", "tasks", "accumulate", "merge", "reduce1", "reduce2", "final"]
+STAGES = ["count", "scan", "scatter", "tasks", "accumulate", "merge", "reduce1", "reduce2",
+          "reduce3", "final"]
 
 
 class MsmOptions(ctypes.Structure):
     _fields_ = [("window_bits", ctypes.c_int32), ("signed_digits", ctypes.c_int32),
                 ("seg_len", ctypes.c_int32), ("red_len_log2", ctypes.c_int32),
-                ("use_graph", ctypes.c_int32), ("mode", ctypes.c_int32)]
+                ("use_graph", ctypes.c_int32), ("mode", ctypes.c_int32),
+                ("fixed_base", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -95,6 +97,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "msm_field_selftest": (ctypes.c_int, [I32, P, P, P, U64]),
         "msm_measure_madd_rate": (ctypes.c_double, [P, I32]),
         "msm_mult_noalloc": (ctypes.c_int, [P, P, U64, U64, P, P]),
+        "msm_measure_int_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -277,6 +280,15 @@ def generate_scalars(seed: int, n: int, kind: int = 0, msm_index: int = 0) -> np
 
 def measure_imad_peak(iters: int = 20000) -> float:
     return load_library().msm_measure_imad_peak(iters)
+
+
+def measure_int_peaks() -> dict:
+    """IMAD-pipe rates (per second): mad.lo/mad.hi pairs, mad.lo only, mad.hi only."""
+    arr = (ctypes.c_double * 3)()
+    n = load_library().msm_measure_int_peaks(arr, 3)
+    if n <= 0:
+        raise MsmError(f"msm_measure_int_peaks: {last_error()}")
+    return {"mad_lo_hi": arr[0], "mad_lo": arr[1], "mad_hi": arr[2]}
 
 
 def device_info() -> str:

@@ -207,7 +207,7 @@ static __device__ __noinline__ wpt_t te_to_weierstrass(const xyzt_t &p) {
   }
   const fq_t zpy = fq_add(p.z, p.y);
   const fq_t zmy = fq_sub(p.z, p.y);
-  const fq_t inv = fq_inv(fq_mul_ool(zmy, p.x));
+  const fq_t inv = fq_inv_vartime(fq_mul_ool(zmy, p.x));
   const fq_t u = fq_mul_ool(fq_mul_ool(zpy, p.x), inv);
   const fq_t v = fq_mul_ool(fq_mul_ool(fq_mul_ool(zpy, p.z), inv), fq_from(ts));
   r.x = fq_add(fq_mul_ool(u, fq_from(icb)), fq_from(ca3));
@@ -224,7 +224,7 @@ static __device__ __noinline__ wpt_t w_normalize(const wpt_t &p) {
     r.y = fq_canon(r.y);
     return r;
   }
-  const fq_t zi = fq_inv(p.z);
+  const fq_t zi = fq_inv_vartime(p.z);
   const fq_t zi2 = fq_sqr_ool(zi);
   wpt_t r;
   r.x = fq_canon(fq_mul_ool(p.x, zi2));

@@ -32,6 +32,9 @@ struct JobDesc {
   uint32_t win_begin;     // first global window id
   uint32_t signed_digits; // 1: signed c-bit digits, 0: unsigned
   uint32_t result_slot;   // index into the pass's result array
+  uint32_t fixed;         // 1: fixed-base tables, every window shares one bucket array
+  uint32_t nred;          // windows of the bucket reduction (1 for fixed-base jobs)
+  uint64_t fb_stride;     // base-table index step from one window's table to the next
 };
 
 // One (MSM, window) pair for the bucket reduction.
@@ -42,6 +45,8 @@ struct WinDesc {
   uint32_t nb;            // buckets in this window
   uint32_t seg_begin;     // first level-1 reduction segment
   uint32_t nseg;          // level-1 segments in this window
+  uint32_t grp_begin;     // first level-2 group (2^grp_len_log2 segments each)
+  uint32_t ngrp;          // level-2 groups in this window
 };
 
 struct Task {             // a run of sorted entries that one thread accumulates
@@ -82,6 +87,8 @@ struct PassBuffers {
   uint32_t n_segs;              // level-1 reduction segments
   uint32_t seg_len;             // max entries per accumulate task
   uint32_t red_len_log2;        // level-1 reduction segment length = 1 << red_len_log2
+  uint32_t grp_len_log2;        // level-2 group = 1 << grp_len_log2 level-1 segments
+  uint32_t n_grps;              // level-2 groups
   uint64_t max_entries;         // capacity of vals
   uint32_t max_tasks;           // capacity of tasks / partials
 
@@ -94,8 +101,11 @@ struct PassBuffers {
   Task *tasks;                  // [max_tasks]
   uint4 *partials;              // [max_tasks] x 12 uint4
   uint32_t *heavy;              // [n_buckets]
+  uint32_t *order;              // [max_tasks] task ids, longest first
+  uint32_t *len_hist;           // [seg_len + 1] task-length histogram, then start cursors
   uint32_t *counters;           // [CNT_WORDS]
   uint4 *seg_out;               // [n_segs] x 2 x 12 uint4
+  uint4 *grp_out;               // [n_grps] x 2 x 12 uint4
   uint4 *win_sum;               // [n_wins] x 12 uint4
   uint64_t *results;            // [n_jobs] x 18 u64 (g1_projective_t)
 };
@@ -104,7 +114,7 @@ struct PassBuffers {
 // `stage_events` (10 events, or null) are recorded around the stages for per-kernel timing
 cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t stream,
                             cudaEvent_t *stage_events);
-#define MSM_NUM_STAGES 9
+#define MSM_NUM_STAGES 10
 size_t msm_scan_tmp_words(uint32_t n_buckets);
 
 // resident-base preparation
@@ -113,6 +123,11 @@ cudaError_t msm_launch_precompute(const void *d_affine, size_t n, uint4 *d_bases
                                   uint32_t index_offset, cudaStream_t stream);
 cudaError_t msm_launch_check_classes(const uint4 *d_class_pts, uint32_t n, uint32_t *d_ok,
                                      cudaStream_t stream);
+// fixed-base tables: bases[(w * n + i)] = 2^(c w) * P_i for w in [1, nwin), from window 0;
+// sets *d_fail when a base's doubling chain leaves the affine curve (a point of 2-power order)
+cudaError_t msm_launch_fixed_base(uint4 *d_bases, const uint8_t *d_flags, uint64_t n, uint64_t first,
+                                  uint64_t count, uint32_t c, uint32_t nwin, uint32_t *d_fail,
+                                  cudaStream_t stream);
 // bases k_i * G with k_i from the seeded generator, written as g1_affine_t
 cudaError_t msm_launch_gen_bases(uint64_t seed, uint64_t first, size_t n, void *d_affine,
                                  const uint4 *d_table, cudaStream_t stream);
@@ -120,7 +135,7 @@ cudaError_t msm_build_gen_table(uint4 *d_table, cudaStream_t stream);
 // self-test hooks
 cudaError_t msm_launch_field_test(int op, const uint32_t *a, const uint32_t *b, uint32_t *out,
                                   size_t n, cudaStream_t stream);
-cudaError_t msm_launch_imad_peak(uint32_t *sink, int blocks, int threads, int iters,
+cudaError_t msm_launch_imad_peak(uint32_t *sink, int blocks, int threads, int iters, int mode,
                                  cudaStream_t stream);
 cudaError_t msm_launch_madd_bench(const uint4 *bases, uint32_t nbases, uint4 *out, int blocks,
                                   int threads, int iters, cudaStream_t stream);

@@ -6,8 +6,9 @@
 // below 2q without a final subtraction.  Addition/subtraction reduce by 2q.  fq_canon() brings a
 // value to [0, q) for comparisons and for the ABI.
 //
-// The multiplier is operand-scanning CIOS on IMAD carry chains (mad.lo/madc.hi with .cc):
-// 4 x 12 multiply-adds plus one m = t0 * (-q^-1) per limb row, 588 IMAD per product.
+// The multiplier is operand-scanning CIOS with 64-bit wide multiply-adds: 12 + 11 limb products
+// per row (q's lowest limb is 1), 276 wide IMADs per product.  The survey's algorithmic count
+// for the roofline stays 588 32-bit IMAD per product (lo and hi halves of 12 x 12 + 12 x 12).
 // The field is the one the reference computes in with GMP (host/msm_compute/include/
 // bls12_377_g1/bls12_377_g1.h:31-33, 90-219); the limb layout is new.
 #pragma once
@@ -32,6 +33,8 @@
 // 1/c_B and c_A/(3 c_B) of the Montgomery -> Weierstrass map (bls12_377_g1.h:366-374)
 #define BLS_INV_CB {0x776b1e1du, 0x455ce02fu, 0x63e0aa56u, 0x4b123b66u, 0x73fa6bf3u, 0x4d75723eu, 0x885e1101u, 0x468df1d4u, 0x638ee120u, 0x039e6c63u, 0x67cb3b82u, 0x005cdbd9u}
 #define BLS_CA_OVER_3CB {0x00000099u, 0x823ac000u, 0xb000004fu, 0xc5cabdc0u, 0x2f8c080du, 0x7f75ae86u, 0x9278b089u, 0x9ed4423bu, 0xec64c452u, 0x79467000u, 0x34c71c50u, 0x0120d3e4u}
+// R^3 mod q: turns a plain inverse of a Montgomery-form value into the Montgomery-form inverse
+#define BLS_R3 {0x8815de20u, 0x581f532fu, 0xbe329585u, 0xe50f4148u, 0x0449f513u, 0x2be8b118u, 0xc804a20eu, 0x6a2a9516u, 0x13590cb9u, 0x3f725407u, 0xc0e7dda5u, 0x01065ab4u}
 // q - 2, the Fermat inversion exponent
 #define BLS_QM2 {0xffffffffu, 0x8508bfffu, 0x30000000u, 0x170b5d44u, 0xba094800u, 0x1ef3622fu, 0x00f5138fu, 0x1a22d9f3u, 0x6ca1493bu, 0xc63b05c0u, 0x17c510eau, 0x01ae3a46u}
 
@@ -115,6 +118,11 @@ __device__ __forceinline__ fq_t fq_one() {
 }
 
 // ---- a * b * 2^-384 mod q (CIOS; inputs and output in [0, 2q)) ----
+// Each limb product is one 32 x 32 -> 64 multiply-add into a 64-bit accumulator whose high word
+// is the next carry; the compiler issues these as wide IMADs.  On GB300 this form runs ~20% faster
+// than mad.lo/madc.hi carry chains, whose high halves issue at half rate.  Because q = 1 mod 2^32
+// and -q^-1 = -1 mod 2^32, the row factor is m = -t0 and m * q0 + t0 = 0 with a carry of
+// (t0 != 0), which saves one product per row.
 __device__ __forceinline__ fq_t fq_mul(const fq_t &a, const fq_t &b) {
   const uint32_t q[FQ_LIMBS] = BLS_Q;
   uint32_t t[FQ_LIMBS + 1];
@@ -122,30 +130,23 @@ __device__ __forceinline__ fq_t fq_mul(const fq_t &a, const fq_t &b) {
   for (int j = 0; j <= FQ_LIMBS; j++) t[j] = 0;
 #pragma unroll
   for (int i = 0; i < FQ_LIMBS; i++) {
-    const uint32_t bi = b.v[i];
-    // t += a * b_i : low halves at j, high halves at j+1 (t[12] is 0 on entry)
-    t[0] = madlo_cc(a.v[0], bi, t[0]);
+    uint64_t acc = 0;
 #pragma unroll
-    for (int j = 1; j < FQ_LIMBS; j++) t[j] = madclo_cc(a.v[j], bi, t[j]);
-    t[FQ_LIMBS] = addc(0u, 0u);
-    t[1] = madhi_cc(a.v[0], bi, t[1]);
+    for (int j = 0; j < FQ_LIMBS; j++) {
+      acc = (uint64_t)a.v[j] * b.v[i] + t[j] + (acc >> 32);
+      t[j] = (uint32_t)acc;
+    }
+    t[FQ_LIMBS] += (uint32_t)(acc >> 32);
+    const uint32_t m = 0u - t[0];
+    acc = (uint64_t)(t[0] != 0u) << 32;
 #pragma unroll
-    for (int j = 1; j < FQ_LIMBS - 1; j++) t[j + 1] = madchi_cc(a.v[j], bi, t[j + 1]);
-    t[FQ_LIMBS] = madchi(a.v[FQ_LIMBS - 1], bi, t[FQ_LIMBS]);
-    // t += m * q with m chosen so that t[0] becomes 0
-    const uint32_t m = t[0] * BLS_QINV;
-    t[0] = madlo_cc(m, q[0], t[0]);
-#pragma unroll
-    for (int j = 1; j < FQ_LIMBS; j++) t[j] = madclo_cc(m, q[j], t[j]);
-    t[FQ_LIMBS] = addc(t[FQ_LIMBS], 0u);
-    t[1] = madhi_cc(m, q[0], t[1]);
-#pragma unroll
-    for (int j = 1; j < FQ_LIMBS - 1; j++) t[j + 1] = madchi_cc(m, q[j], t[j + 1]);
-    t[FQ_LIMBS] = madchi(m, q[FQ_LIMBS - 1], t[FQ_LIMBS]);
-    // divide by 2^32
-#pragma unroll
-    for (int j = 0; j < FQ_LIMBS; j++) t[j] = t[j + 1];
-    t[FQ_LIMBS] = 0;
+    for (int j = 1; j < FQ_LIMBS; j++) {
+      acc = (uint64_t)m * q[j] + t[j] + (acc >> 32);
+      t[j - 1] = (uint32_t)acc;
+    }
+    acc = (uint64_t)t[FQ_LIMBS] + (acc >> 32);
+    t[FQ_LIMBS - 1] = (uint32_t)acc;
+    t[FQ_LIMBS] = (uint32_t)(acc >> 32);
   }
   fq_t r;
 #pragma unroll
@@ -259,6 +260,102 @@ static __device__ __noinline__ fq_t fq_inv(const fq_t &a) {
     }
   }
   return r;
+}
+
+// ---- variable-time inversion by the binary extended Euclidean algorithm ----
+// For the serial tail of a pass (one thread): about 2 x 377 shift/subtract steps on 12 limbs,
+// an order of magnitude shorter than the ~480 dependent products of fq_inv.  The running time
+// depends on the value, which is fine here: nothing in an MSM is secret.
+__device__ __forceinline__ bool big_is_one(const uint32_t (&x)[FQ_LIMBS]) {
+  uint32_t acc = x[0] ^ 1u;
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) acc |= x[j];
+  return acc == 0;
+}
+__device__ __forceinline__ void big_shr1(uint32_t (&x)[FQ_LIMBS]) {
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS - 1; j++) x[j] = __funnelshift_r(x[j], x[j + 1], 1);
+  x[FQ_LIMBS - 1] >>= 1;
+}
+// x = x / 2 mod q for x < q (adds q first when x is odd; x + q < 2^384)
+__device__ __forceinline__ void half_mod_q(uint32_t (&x)[FQ_LIMBS]) {
+  const uint32_t q[FQ_LIMBS] = BLS_Q;
+  if (x[0] & 1u) {
+    x[0] = add_cc(x[0], q[0]);
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS - 1; j++) x[j] = addc_cc(x[j], q[j]);
+    x[FQ_LIMBS - 1] = addc(x[FQ_LIMBS - 1], q[FQ_LIMBS - 1]);
+  }
+  big_shr1(x);
+}
+// x = x - y mod q for x, y < q
+__device__ __forceinline__ void sub_mod_q(uint32_t (&x)[FQ_LIMBS], const uint32_t (&y)[FQ_LIMBS]) {
+  const uint32_t q[FQ_LIMBS] = BLS_Q;
+  x[0] = sub_cc(x[0], y[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) x[j] = subc_cc(x[j], y[j]);
+  const uint32_t mask = subc(0u, 0u);
+  x[0] = add_cc(x[0], q[0] & mask);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) x[j] = addc_cc(x[j], q[j] & mask);
+  x[FQ_LIMBS - 1] = addc(x[FQ_LIMBS - 1], q[FQ_LIMBS - 1] & mask);
+}
+// returns true when x >= y
+__device__ __forceinline__ bool big_geq(const uint32_t (&x)[FQ_LIMBS], const uint32_t (&y)[FQ_LIMBS]) {
+  sub_cc(x[0], y[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) subc_cc(x[j], y[j]);
+  return subc(0u, 0u) == 0u;
+}
+__device__ __forceinline__ void big_sub(uint32_t (&x)[FQ_LIMBS], const uint32_t (&y)[FQ_LIMBS]) {
+  x[0] = sub_cc(x[0], y[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) x[j] = subc_cc(x[j], y[j]);
+  x[FQ_LIMBS - 1] = subc(x[FQ_LIMBS - 1], y[FQ_LIMBS - 1]);
+}
+
+// Montgomery-form inverse (0 -> 0).  With a = xR, the integer inverse of a times R^3 through one
+// Montgomery product gives x^-1 R.
+static __device__ __noinline__ fq_t fq_inv_vartime(const fq_t &a) {
+  const fq_t c = fq_canon(a);
+  uint32_t u[FQ_LIMBS], v[FQ_LIMBS], x1[FQ_LIMBS], x2[FQ_LIMBS];
+  const uint32_t q[FQ_LIMBS] = BLS_Q;
+  uint32_t nz = 0;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) {
+    u[j] = c.v[j];
+    v[j] = q[j];
+    x1[j] = 0;
+    x2[j] = 0;
+    nz |= c.v[j];
+  }
+  if (!nz) return fq_zero();
+  x1[0] = 1;
+#pragma unroll 1
+  for (int guard = 0; guard < 4 * 384; guard++) {
+    if (big_is_one(u) || big_is_one(v)) break;
+    for (int k = 0; k < 384 && !(u[0] & 1u); k++) {  // u, v stay nonzero: gcd(a, q) = 1
+      big_shr1(u);
+      half_mod_q(x1);
+    }
+    for (int k = 0; k < 384 && !(v[0] & 1u); k++) {
+      big_shr1(v);
+      half_mod_q(x2);
+    }
+    if (big_geq(u, v)) {
+      big_sub(u, v);
+      sub_mod_q(x1, x2);
+    } else {
+      big_sub(v, u);
+      sub_mod_q(x2, x1);
+    }
+  }
+  fq_t inv;
+  const bool use1 = big_is_one(u);
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) inv.v[j] = use1 ? x1[j] : x2[j];
+  const uint32_t r3[FQ_LIMBS] = BLS_R3;
+  return fq_mul(inv, fq_from(r3));
 }
 
 // ---- 16-byte vector loads/stores of field elements ----

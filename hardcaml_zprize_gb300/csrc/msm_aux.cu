@@ -43,7 +43,7 @@ __device__ __forceinline__ bool weierstrass_to_pre(const fq_t &x, const fq_t &y,
   const fq_t v = fq_mul_ool(fq_from(ws), y);
   const fq_t up1 = fq_add(u, one);
   if (fq_is_zero(v) || fq_is_zero(up1)) return false;
-  const fq_t inv = fq_inv(fq_mul_ool(v, up1));
+  const fq_t inv = fq_inv_vartime(fq_mul_ool(v, up1));
   const fq_t xe = fq_mul_ool(fq_mul_ool(fq_mul_ool(fq_from(ts), u), up1), inv);
   const fq_t ye = fq_mul_ool(fq_mul_ool(fq_sub(u, one), v), inv);
   out.ymx = fq_canon(fq_mul_ool(fq_sub(ye, xe), fq_from(inv2)));
@@ -101,6 +101,62 @@ __global__ void k_check_classes(const uint4 *pts, uint32_t n, uint32_t *ok) {
   ok[i] = (fq_eq(lhs, rhs) && fq_is_zero(q.z)) ? 1u : 0u;
 }
 
+// Fixed-base tables: for every base P_i (window 0 of the table), the multiples 2^(c w) P_i for
+// w = 1 .. nwin - 1 in the same precomputed form.  One thread per base walks the doubling chain
+// and converts all windows to affine with one batched inversion (Montgomery's trick).
+constexpr int kMaxFbWindows = 24;
+
+__global__ void __launch_bounds__(128) k_fixed_base(uint4 *bases, const uint8_t *flags, uint64_t n,
+                                                    uint64_t first, uint64_t count, uint32_t c,
+                                                    uint32_t nwin, uint32_t *fail) {
+  const uint64_t i = first + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= first + count || i >= n || nwin > kMaxFbWindows) return;
+  if (flags[i] != BASE_OK) {
+    pre_t z;
+    z.ymx = fq_zero();
+    z.ypx = fq_zero();
+    z.kt = fq_zero();
+    for (uint32_t w = 1; w < nwin; w++) pre_store(bases + ((size_t)w * n + i) * 9, z);
+    return;
+  }
+  pre_t p0;
+  pre_load(p0, bases + i * 9);
+  xyzt_t P;
+  P.x = fq_sub(p0.ypx, p0.ymx);  // (y+x)/2 - (y-x)/2
+  P.y = fq_add(p0.ypx, p0.ymx);
+  P.z = fq_one();
+  P.t = fq_mul_ool(P.x, P.y);
+  fq_t X[kMaxFbWindows], Y[kMaxFbWindows], Z[kMaxFbWindows], pre[kMaxFbWindows];
+  fq_t acc = fq_one();
+#pragma unroll 1
+  for (uint32_t w = 1; w < nwin; w++) {
+#pragma unroll 1
+    for (uint32_t k = 0; k < c; k++) P = te_dbl_ool(P);
+    X[w] = P.x;
+    Y[w] = P.y;
+    Z[w] = P.z;
+    pre[w] = acc;  // product of Z[1 .. w-1]
+    acc = fq_mul_ool(acc, P.z);
+  }
+  if (fq_is_zero(acc)) {  // some 2^j P left the affine curve: P has 2-power order
+    atomicAdd(fail, 1u);
+    return;
+  }
+  fq_t inv = fq_inv_vartime(acc);
+  const uint32_t inv2[FQ_LIMBS] = BLS_INV2, dd[FQ_LIMBS] = BLS_TE_D;
+#pragma unroll 1
+  for (uint32_t w = nwin - 1; w >= 1; w--) {
+    const fq_t zi = fq_mul_ool(inv, pre[w]);
+    inv = fq_mul_ool(inv, Z[w]);
+    const fq_t x = fq_mul_ool(X[w], zi), y = fq_mul_ool(Y[w], zi);
+    pre_t q;
+    q.ymx = fq_canon(fq_mul_ool(fq_sub(y, x), fq_from(inv2)));
+    q.ypx = fq_canon(fq_mul_ool(fq_add(y, x), fq_from(inv2)));
+    q.kt = fq_canon(fq_mul_ool(fq_mul_ool(x, y), fq_from(dd)));
+    pre_store(bases + ((size_t)w * n + i) * 9, q);
+  }
+}
+
 // ---- seeded generator: SplitMix64 (Steele, Lea, Flood 2014), counter-based ----
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   uint64_t z = x + 0x9E3779B97F4A7C15ull;
@@ -140,7 +196,7 @@ __global__ void k_gen_table(uint4 *table) {
   }
   // affine twisted Edwards, then the precomputed form
   const uint32_t inv2[FQ_LIMBS] = BLS_INV2, dd[FQ_LIMBS] = BLS_TE_D;
-  const fq_t zi = fq_inv(acc.z);
+  const fq_t zi = fq_inv_vartime(acc.z);
   const fq_t x = fq_mul_ool(acc.x, zi), y = fq_mul_ool(acc.y, zi);
   pre_t p;
   p.ymx = fq_canon(fq_mul_ool(fq_sub(y, x), fq_from(inv2)));
@@ -194,13 +250,16 @@ __global__ void k_field_test(int op, const uint32_t *a, const uint32_t *b, uint3
     case 3: r = fq_inv(x); break;
     case 4: r = fq_canon(x); break;
     case 5: r = fq_neg(x); break;
+    case 6: r = fq_inv_vartime(x); break;
     default: r = fq_zero(); break;
   }
 #pragma unroll
   for (int k = 0; k < FQ_LIMBS; k++) out[i * FQ_LIMBS + k] = r.v[k];
 }
 
-// Peak IMAD rate: 8 independent mad.lo / mad.hi chains per thread.
+// Peak IMAD rates: 8 independent chains per thread of mad.lo/mad.hi pairs (mode 0), mad.lo only
+// (mode 1) or mad.hi only (mode 2); 16 IMAD per chain step.
+template <int MODE>
 __global__ void k_imad_peak(uint32_t *sink, int iters) {
   uint32_t a[8], b = threadIdx.x | 1u, c = blockIdx.x * 2654435761u;
 #pragma unroll
@@ -209,8 +268,16 @@ __global__ void k_imad_peak(uint32_t *sink, int iters) {
   for (int it = 0; it < iters; it++) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
-      asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+      if (MODE == 0) {
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+        asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+      } else if (MODE == 1) {
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+      } else {
+        asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+        asm volatile("mad.hi.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"(c));
+      }
     }
   }
   uint32_t s = 0;
@@ -246,6 +313,16 @@ cudaError_t msm_launch_precompute(const void *d_affine, size_t n, uint4 *d_bases
   return cudaGetLastError();
 }
 
+cudaError_t msm_launch_fixed_base(uint4 *d_bases, const uint8_t *d_flags, uint64_t n, uint64_t first,
+                                  uint64_t count, uint32_t c, uint32_t nwin, uint32_t *d_fail,
+                                  cudaStream_t st) {
+  if (count == 0 || nwin <= 1) return cudaSuccess;
+  if (nwin > kMaxFbWindows) return cudaErrorInvalidValue;
+  k_fixed_base<<<(unsigned)((count + 127) / 128), 128, 0, st>>>(d_bases, d_flags, n, first, count, c,
+                                                               nwin, d_fail);
+  return cudaGetLastError();
+}
+
 cudaError_t msm_launch_check_classes(const uint4 *d_pts, uint32_t n, uint32_t *d_ok, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_check_classes<<<1, 32, 0, st>>>(d_pts, n, d_ok);
@@ -271,8 +348,11 @@ cudaError_t msm_launch_field_test(int op, const uint32_t *a, const uint32_t *b, 
   return cudaGetLastError();
 }
 
-cudaError_t msm_launch_imad_peak(uint32_t *sink, int blocks, int threads, int iters, cudaStream_t st) {
-  k_imad_peak<<<blocks, threads, 0, st>>>(sink, iters);
+cudaError_t msm_launch_imad_peak(uint32_t *sink, int blocks, int threads, int iters, int mode,
+                                 cudaStream_t st) {
+  if (mode == 1) k_imad_peak<1><<<blocks, threads, 0, st>>>(sink, iters);
+  else if (mode == 2) k_imad_peak<2><<<blocks, threads, 0, st>>>(sink, iters);
+  else k_imad_peak<0><<<blocks, threads, 0, st>>>(sink, iters);
   return cudaGetLastError();
 }
 

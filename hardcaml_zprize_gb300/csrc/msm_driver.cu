@@ -128,8 +128,11 @@ struct Cfg {
   uint32_t c = 16;
   uint32_t signed_digits = 1;
   uint32_t seg_len = 1024;
-  uint32_t red_log2 = 5;
+  uint32_t red_log2 = 4;
+  uint32_t fixed = 0;  // use the context's fixed-base tables (c is then the tables' width)
 };
+
+constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
 
 uint32_t windows_of(uint32_t c) { return (MSM_SCALAR_BITS + c - 1) / c; }
 
@@ -153,12 +156,21 @@ void layout(uint32_t c, uint32_t sgn, uint32_t &nwin, uint32_t &nb, uint32_t &nb
   }
 }
 
-// cost model in 12-limb multiplications: 7 per bucket add, 18 per bucket in the reduction
+// Cost model in 12-limb products at throughput: 7 per bucket add, 18 per bucket in the
+// reduction, and the serial window combine of the standard layout, c doublings per window at
+// two product latencies each (one product latency ~ 12.6k products of throughput on GB300).
 double model_cost(uint64_t n, uint32_t c, uint32_t sgn) {
   uint32_t nwin, nb, nbt;
   layout(c, sgn, nwin, nb, nbt);
   const double buckets = (double)(nwin - 1) * nb + nbt;
-  return (double)n * nwin * 7.0 + buckets * 18.0 + (double)nwin * 4000.0;
+  return (double)n * nwin * 7.0 + buckets * 18.0 + (double)(nwin - 1) * c * 2.0 * 12600.0;
+}
+double model_cost_fixed(uint64_t n, uint32_t c, uint32_t sgn) {
+  uint32_t nwin, nb, nbt;
+  layout(c, sgn, nwin, nb, nbt);
+  // 18 products per bucket in level 1, plus the level-2/3 combines and the bucket metadata
+  // passes, measured at about a third more per bucket
+  return (double)n * nwin * 7.0 + (double)std::max(nb, nbt) * 24.0;
 }
 
 Cfg heuristic_cfg(uint64_t n) {
@@ -177,10 +189,15 @@ Cfg heuristic_cfg(uint64_t n) {
   uint32_t s = 32;
   while (s < 2 * mean && s < 4096) s <<= 1;
   cfg.seg_len = s;
-  // level-1 segment length L with 2L ~ 3 nb / (128 L) adds per thread on both levels
-  const double l = std::sqrt(3.0 * nb / 256.0);
-  cfg.red_log2 = std::min<uint32_t>(std::max<uint32_t>(log2_ceil((uint64_t)std::max(1.0, l)), 2), 10);
+  cfg.red_log2 = 4;
   return cfg;
+}
+
+uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing) {
+  const double mean = (double)n * nwin_sharing / std::max<uint32_t>(nb, 1);
+  uint32_t s = 32;
+  while (s < 2 * mean && s < 4096) s <<= 1;
+  return s;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -189,13 +206,14 @@ Cfg heuristic_cfg(uint64_t n) {
 struct JobSpec {
   uint64_t n, base_off, scalar_off;
   Cfg cfg;
+  uint64_t fb_stride = 0;  // fixed-base jobs: index step between the windows' tables
 };
 
 struct Plan {
   std::vector<JobDesc> jobs;
   std::vector<WinDesc> wins;
   uint64_t n_points = 0, max_entries = 0;
-  uint32_t n_buckets = 0, n_segs = 0, max_tasks = 0;
+  uint32_t n_buckets = 0, n_segs = 0, n_grps = 0, max_tasks = 0;
   uint32_t seg_len = 1024, red_log2 = 5;
   std::string key;
 };
@@ -205,7 +223,7 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   if (specs.empty()) return fail(ERR_ARG, "empty pass");
   pl.seg_len = specs[0].cfg.seg_len;
   pl.red_log2 = specs[0].cfg.red_log2;
-  uint64_t buckets = 0, segs = 0, wins = 0;
+  uint64_t buckets = 0, segs = 0, wins = 0, grps = 0;
   char tmp[160];
   for (size_t j = 0; j < specs.size(); j++) {
     const JobSpec &s = specs[j];
@@ -224,26 +242,34 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
       d.nb = d.nb_top = 0;
     } else {
       layout(d.c, d.signed_digits, d.nwin, d.nb, d.nb_top);
+      d.fixed = s.cfg.fixed;
+      d.fb_stride = s.fb_stride;
+      d.nred = d.fixed ? 1 : d.nwin;
       const uint32_t L = 1u << pl.red_log2;
-      for (uint32_t w = 0; w < d.nwin; w++) {
+      for (uint32_t w = 0; w < d.nred; w++) {
         WinDesc wd{};
         wd.job = (uint32_t)j;
         wd.w = w;
         wd.bucket_begin = (uint32_t)(buckets + (uint64_t)w * d.nb);
-        wd.nb = (w + 1 == d.nwin) ? d.nb_top : d.nb;
+        wd.nb = d.fixed ? std::max(d.nb, d.nb_top) : (w + 1 == d.nwin) ? d.nb_top : d.nb;
         wd.seg_begin = (uint32_t)segs;
         wd.nseg = (wd.nb + L - 1) / L;
+        wd.grp_begin = (uint32_t)grps;
+        wd.ngrp = (wd.nseg + (1u << kGrpLenLog2) - 1) >> kGrpLenLog2;
         segs += wd.nseg;
+        grps += wd.ngrp;
         pl.wins.push_back(wd);
       }
-      buckets += (uint64_t)(d.nwin - 1) * d.nb + d.nb_top;
-      wins += d.nwin;
+      buckets += d.fixed ? (uint64_t)std::max(d.nb, d.nb_top)
+                         : (uint64_t)(d.nwin - 1) * d.nb + d.nb_top;
+      wins += d.nred;
       pl.max_entries += s.n * d.nwin;
     }
     pl.n_points += s.n;
     pl.jobs.push_back(d);
-    snprintf(tmp, sizeof(tmp), "%llu/%llu/%llu/%u/%u;", (unsigned long long)s.n,
-             (unsigned long long)s.base_off, (unsigned long long)s.scalar_off, d.c, d.signed_digits);
+    snprintf(tmp, sizeof(tmp), "%llu/%llu/%llu/%u/%u/%u;", (unsigned long long)s.n,
+             (unsigned long long)s.base_off, (unsigned long long)s.scalar_off, d.c, d.signed_digits,
+             d.fixed);
     pl.key += tmp;
   }
   if (buckets >= (1ull << 32) || pl.max_entries >= (1ull << 32) - 1 || segs >= (1ull << 31))
@@ -251,6 +277,7 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
                 (unsigned long long)buckets, (unsigned long long)pl.max_entries);
   pl.n_buckets = (uint32_t)buckets;
   pl.n_segs = (uint32_t)segs;
+  pl.n_grps = (uint32_t)grps;
   const uint64_t mt = buckets + pl.max_entries / pl.seg_len + 1;
   if (mt >= (1ull << 31)) return fail(ERR_BUDGET, "too many tasks");
   pl.max_tasks = (uint32_t)mt;
@@ -264,8 +291,8 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
   uint64_t b = 0;
   b += (uint64_t)pl.n_buckets * 4 * 5;                   // count, offset, fill, taskoff, heavy
   b += pl.max_entries * 4;                                // vals
-  b += (uint64_t)pl.max_tasks * (sizeof(Task) + MSM_BUCKET_BYTES);
-  b += (uint64_t)pl.n_segs * 2 * MSM_BUCKET_BYTES;
+  b += (uint64_t)pl.max_tasks * (sizeof(Task) + 4 + MSM_BUCKET_BYTES);
+  b += (uint64_t)(pl.n_segs + pl.n_grps) * 2 * MSM_BUCKET_BYTES;
   b += (uint64_t)pl.wins.size() * MSM_BUCKET_BYTES;
   b += pl.jobs.size() * (sizeof(JobDesc) + MSM_PROJ_BYTES) + pl.wins.size() * sizeof(WinDesc);
   if (with_scalars) b += pl.n_points * 32;
@@ -277,10 +304,10 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
 // ---------------------------------------------------------------------------------------------
 struct Workspace {
   DevBuf count, offset, fill, taskoff, scan_tmp, vals, tasks, partials, heavy, counters, seg_out,
-      win_sum, results, jobs, wins;
+      grp_out, win_sum, results, jobs, wins, order, len_hist;
   DevBuf scalars[2];
   HostPinned res_host;
-  cudaEvent_t ev[10] = {};
+  cudaEvent_t ev[MSM_NUM_STAGES + 1] = {};
   uint64_t generation = 0;  // bumps when any buffer moves (graphs must be re-captured)
   std::unordered_map<std::string, cudaGraphExec_t> graphs;
 
@@ -300,8 +327,11 @@ struct Workspace {
     CK(vals.ensure((size_t)pl.max_entries * 4, &moved));
     CK(tasks.ensure((size_t)pl.max_tasks * sizeof(Task), &moved));
     CK(partials.ensure((size_t)pl.max_tasks * MSM_BUCKET_BYTES, &moved));
+    CK(order.ensure((size_t)pl.max_tasks * 4, &moved));
+    CK(len_hist.ensure((size_t)(pl.seg_len + 1) * 4, &moved));
     CK(counters.ensure(CNT_WORDS * 4, &moved));
     CK(seg_out.ensure((size_t)pl.n_segs * 2 * MSM_BUCKET_BYTES, &moved));
+    CK(grp_out.ensure((size_t)pl.n_grps * 2 * MSM_BUCKET_BYTES, &moved));
     CK(win_sum.ensure(pl.wins.size() * MSM_BUCKET_BYTES, &moved));
     CK(results.ensure(pl.jobs.size() * MSM_PROJ_BYTES, &moved));
     CK(jobs.ensure(pl.jobs.size() * sizeof(JobDesc), &moved));
@@ -321,6 +351,7 @@ struct Workspace {
     graphs.clear();
     count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
     scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
+    order.release(); len_hist.release(); grp_out.release();
     win_sum.release(); scalars[0].release(); scalars[1].release();
     generation++;
   }
@@ -333,6 +364,7 @@ struct Ctx {
   int device = 0;
   int num_sms = 0;
   uint64_t npoints = 0;
+  uint32_t fb_c = 0, fb_w = 1;  // fixed-base tables: window width and windows (fb_c 0: none)
   DevBuf bases, flags, special_idx, special_cls, class_pts;
   uint32_t n_special = 0, n_classes = 0;
   cudaStream_t stream = nullptr, copy_stream = nullptr;
@@ -362,7 +394,7 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.class_pts = cx->class_pts.as<uint4>();
   pb.n_special = cx->n_special;
   pb.n_classes = cx->n_classes;
-  pb.n_bases = cx->npoints;
+  pb.n_bases = cx->npoints * cx->fb_w;
   pb.scalars = (const uint4 *)d_scalars;
   pb.jobs = ws.jobs.as<JobDesc>();
   pb.wins = ws.wins.as<WinDesc>();
@@ -371,8 +403,10 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.n_points = pl.n_points;
   pb.n_buckets = pl.n_buckets;
   pb.n_segs = pl.n_segs;
+  pb.n_grps = pl.n_grps;
   pb.seg_len = pl.seg_len;
   pb.red_len_log2 = pl.red_log2;
+  pb.grp_len_log2 = kGrpLenLog2;
   pb.max_entries = pl.max_entries;
   pb.max_tasks = pl.max_tasks;
   pb.count = ws.count.as<uint32_t>();
@@ -384,8 +418,11 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.tasks = ws.tasks.as<Task>();
   pb.partials = ws.partials.as<uint4>();
   pb.heavy = ws.heavy.as<uint32_t>();
+  pb.order = ws.order.as<uint32_t>();
+  pb.len_hist = ws.len_hist.as<uint32_t>();
   pb.counters = ws.counters.as<uint32_t>();
   pb.seg_out = ws.seg_out.as<uint4>();
+  pb.grp_out = ws.grp_out.as<uint4>();
   pb.win_sum = ws.win_sum.as<uint4>();
   pb.results = ws.results.as<uint64_t>();
   return pb;
@@ -453,25 +490,39 @@ Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
   Cfg cfg = heuristic_cfg(n);
   auto it = cx->tuned.find(log2_ceil(std::max<uint64_t>(n, 1)));
   if (it != cx->tuned.end()) cfg = it->second;
+  const bool forced_c = opt && opt->window_bits > 0;
   if (opt) {
-    if (opt->window_bits > 0) {
+    if (forced_c) {
       cfg.c = (uint32_t)std::min(std::max(opt->window_bits, 4), 22);
       uint32_t nwin, nb, nbt;
       layout(cfg.c, 1, nwin, nb, nbt);
-      const double mean = (double)n / nb;
-      uint32_t s = 32;
-      while (s < 2 * mean && s < 4096) s <<= 1;
-      cfg.seg_len = s;
-      const double l = std::sqrt(3.0 * nb / 256.0);
-      cfg.red_log2 =
-          std::min<uint32_t>(std::max<uint32_t>(log2_ceil((uint64_t)std::max(1.0, l)), 2), 10);
+      cfg.seg_len = seg_len_for(n, nb, 1);
     }
     if (opt->signed_digits == 1) cfg.signed_digits = 1;
     if (opt->signed_digits == 2) cfg.signed_digits = 0;
-    if (opt->seg_len > 0) cfg.seg_len = (uint32_t)opt->seg_len;
-    if (opt->red_len_log2 > 0) cfg.red_log2 = (uint32_t)std::min(opt->red_len_log2, 12);
   }
   if (!cfg.signed_digits && cfg.c > 21) cfg.c = 21;
+  cfg.fixed = 0;
+  // fixed-base tables: every window shares one bucket array and there is no serial window
+  // combine; chosen when the cost model says so (or when asked)
+  const int fb = opt ? opt->fixed_base : 0;
+  if (cx->fb_c && fb != 2 && (fb == 1 || !forced_c)) {
+    const double cf = model_cost_fixed(n, cx->fb_c, 1);
+    const double cs = model_cost(n, cfg.c, cfg.signed_digits);
+    if (fb == 1 || cf < cs) {
+      uint32_t nwin, nb, nbt;
+      layout(cx->fb_c, 1, nwin, nb, nbt);
+      cfg.fixed = 1;
+      cfg.c = cx->fb_c;
+      cfg.signed_digits = 1;
+      cfg.seg_len = seg_len_for(n, std::max(nb, nbt), nwin);
+      cfg.red_log2 = 4;
+    }
+  }
+  if (opt) {
+    if (opt->seg_len > 0) cfg.seg_len = (uint32_t)std::min(opt->seg_len, 4096);
+    if (opt->red_len_log2 > 0) cfg.red_log2 = (uint32_t)std::min(opt->red_len_log2, 12);
+  }
   return cfg;
 }
 
@@ -510,6 +561,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
       specs[j] = {sizes[j], offs[j], first[j], resolve_cfg(cx, sizes[j], opt)};
       specs[j].cfg.seg_len = resolve_cfg(cx, maxn, opt).seg_len;
       specs[j].cfg.red_log2 = resolve_cfg(cx, maxn, opt).red_log2;
+      specs[j].fb_stride = specs[j].cfg.fixed ? cx->npoints : 0;
     }
     Plan pl;
     if (build_plan(specs, pl)) return g_err;
@@ -536,6 +588,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     uint64_t maxn = 0;
     for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
     one[0] = {maxn, 0, 0, resolve_cfg(cx, maxn, opt)};
+    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
     if (build_plan(one, probe)) return g_err;
     if (ws.ensure(probe)) return g_err;
   }
@@ -547,6 +600,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
   for (size_t j = 0; j < m; j++) {
     std::vector<JobSpec> one(1);
     one[0] = {sizes[j], offs[j], d_scalars ? first[j] : 0, resolve_cfg(cx, sizes[j], opt)};
+    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
     Plan pl;
     if (build_plan(one, pl)) return g_err;
     const void *src = d_scalars;
@@ -594,9 +648,48 @@ int init_device(Ctx *cx) {
   return 0;
 }
 
+// Width of the fixed-base tables for n resident bases (0: none).  MSM_FIXED_BASE=0 turns them
+// off, MSM_FIXED_BASE=<c> forces window width c; by default they are built for n >= 2^20 when
+// n * W * 144 bytes fit in MSM_FIXED_BASE_MAX_GB (default 160) and leave 16 GiB of HBM free.
+uint32_t choose_fixed_base(uint64_t n) {
+  const char *e = getenv("MSM_FIXED_BASE");
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+  double budget = 160.0 * (1ull << 30);
+  if (const char *g = getenv("MSM_FIXED_BASE_MAX_GB")) budget = atof(g) * (1ull << 30);
+  budget = std::min(budget, (double)free_b - 16.0 * (1ull << 30));
+  auto fits = [&](uint32_t c) {
+    const uint32_t w = windows_of(c);
+    return w <= 24 && MSM_SCALAR_BITS % c != 0 && (double)n * w * MSM_BASE_BYTES <= budget &&
+           (double)n * w < 2147483647.0;
+  };
+  if (e) {
+    if (!strcmp(e, "0") || !strcmp(e, "off")) return 0;
+    const int c = atoi(e);
+    if (c >= 11 && c <= 24 && MSM_SCALAR_BITS % c != 0 && windows_of(c) <= 24 &&
+        (double)n * windows_of(c) < 2147483647.0)
+      return (uint32_t)c;
+    if (strcmp(e, "auto")) return 0;
+  }
+  if (n < (1ull << 20)) return 0;
+  uint32_t best = 0;
+  double best_cost = 1e300;
+  for (uint32_t c = 11; c <= 24; c++) {
+    if (!fits(c)) continue;
+    const double v = model_cost_fixed(n, c, 1);
+    if (v < best_cost) {
+      best_cost = v;
+      best = c;
+    }
+  }
+  return best;
+}
+
 int load_bases(Ctx *cx, const g1_affine_t *points, uint64_t n) {
   cx->npoints = n;
-  CK(cx->bases.ensure(std::max<uint64_t>(n, 1) * MSM_BASE_BYTES));
+  cx->fb_c = choose_fixed_base(n);
+  cx->fb_w = cx->fb_c ? windows_of(cx->fb_c) : 1;
+  CK(cx->bases.ensure(std::max<uint64_t>(n, 1) * cx->fb_w * MSM_BASE_BYTES));
   CK(cx->flags.ensure(std::max<uint64_t>(n, 1)));
   CK(cx->special_idx.ensure(std::max<uint64_t>(n, 1) * 4));
   DevBuf cnt, staging;
@@ -611,6 +704,23 @@ int load_bases(Ctx *cx, const g1_affine_t *points, uint64_t n) {
     CK(msm_launch_precompute(staging.p, k, cx->bases.as<uint4>() + i0 * 9,
                              cx->flags.as<uint8_t>() + i0, cx->special_idx.as<uint32_t>(),
                              cnt.as<uint32_t>(), (uint32_t)i0, cx->stream));
+  }
+  if (cx->fb_c) {
+    DevBuf fb_fail;
+    CK(fb_fail.ensure(4));
+    CK(cudaMemsetAsync(fb_fail.p, 0, 4, cx->stream));
+    const uint64_t fchunk = 1ull << 20;
+    for (uint64_t i0 = 0; i0 < n; i0 += fchunk)
+      CK(msm_launch_fixed_base(cx->bases.as<uint4>(), cx->flags.as<uint8_t>(), n, i0,
+                               std::min(fchunk, n - i0), cx->fb_c, cx->fb_w,
+                               fb_fail.as<uint32_t>(), cx->stream));
+    uint32_t nfail = 0;
+    CK(cudaMemcpyAsync(&nfail, fb_fail.p, 4, cudaMemcpyDeviceToHost, cx->stream));
+    CK(cudaStreamSynchronize(cx->stream));
+    if (nfail) {  // a base of 2-power order: keep the plain table only
+      cx->fb_c = 0;
+      cx->fb_w = 1;
+    }
   }
   uint32_t nspecial = 0;
   CK(cudaMemcpyAsync(&nspecial, cnt.p, 4, cudaMemcpyDeviceToHost, cx->stream));
@@ -766,6 +876,7 @@ struct Server {
   uint64_t request_bytes(uint64_t n) {
     std::vector<JobSpec> one(1);
     one[0] = {n, 0, 0, resolve_cfg(cx, n, nullptr)};
+    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
     Plan pl;
     if (build_plan(one, pl)) return ~0ull;
     return plan_bytes(pl, true);
@@ -829,6 +940,7 @@ void Server::loop() {
           specs[j] = {batch[j]->n, batch[j]->base_off, first, resolve_cfg(cx, batch[j]->n, nullptr)};
           specs[j].cfg.seg_len = big.seg_len;
           specs[j].cfg.red_log2 = big.red_log2;
+          specs[j].fb_stride = specs[j].cfg.fixed ? cx->npoints : 0;
           first += batch[j]->n;
         }
         Slot &sl = *free_slot;
@@ -977,6 +1089,7 @@ int msm_get_config(void *context, uint64_t npoints, msm_options_t *out) {
   out->red_len_log2 = (int32_t)c.red_log2;
   out->use_graph = 0;
   out->mode = 1;
+  out->fixed_base = c.fixed ? 1 : 2;
   return 0;
 }
 
@@ -1081,6 +1194,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
     best_out->red_len_log2 = (int32_t)best.red_log2;
     best_out->use_graph = 0;
     best_out->mode = 1;
+    best_out->fixed_base = 2;
   }
   return 0;
 }
@@ -1227,32 +1341,44 @@ int msm_generate_scalars(uint64_t seed, uint64_t n, int32_t kind, uint64_t msm_i
   return 0;
 }
 
-double msm_measure_imad_peak(int32_t iters) {
+int msm_measure_int_peaks(double *rates, int32_t n) {
   const char *dev = getenv("MSM_DEVICE");
-  if (cudaSetDevice(dev ? atoi(dev) : 0) != cudaSuccess) return -1;
+  if (!rates || n <= 0) return fail(ERR_ARG, "null argument");
+  CK(cudaSetDevice(dev ? atoi(dev) : 0));
   cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, dev ? atoi(dev) : 0) != cudaSuccess) return -1;
-  if (iters <= 0) iters = 20000;
+  CK(cudaGetDeviceProperties(&prop, dev ? atoi(dev) : 0));
   DevBuf sink;
-  if (sink.ensure(16) != cudaSuccess) return -1;
-  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  CK(sink.ensure(16));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8, iters = 8000;
   cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  double best = 0;
-  for (int rep = 0; rep < 4; rep++) {
-    cudaEventRecord(e0);
-    msm_launch_imad_peak(sink.as<uint32_t>(), blocks, threads, iters, 0);
-    cudaEventRecord(e1);
-    if (cudaEventSynchronize(e1) != cudaSuccess) return -1;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    const double ops = (double)blocks * threads * iters * 16.0;
-    if (rep > 0) best = std::max(best, ops / (ms * 1e-3));
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  // about 200 ms of warm-up so the clocks settle before timing
+  for (int k = 0; k < 40; k++) msm_launch_imad_peak(sink.as<uint32_t>(), blocks, threads, iters, 0, 0);
+  CK(cudaDeviceSynchronize());
+  const int modes = std::min<int>(n, 3);
+  for (int mode = 0; mode < modes; mode++) {
+    double best = 0;
+    for (int rep = 0; rep < 5; rep++) {
+      cudaEventRecord(e0);
+      msm_launch_imad_peak(sink.as<uint32_t>(), blocks, threads, iters, mode, 0);
+      cudaEventRecord(e1);
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best = std::max(best, (double)blocks * threads * iters * 16.0 / (ms * 1e-3));
+    }
+    rates[mode] = best;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return best;
+  return modes;
+}
+
+double msm_measure_imad_peak(int32_t iters) {
+  (void)iters;
+  double r[1] = {0};
+  return msm_measure_int_peaks(r, 1) == 1 ? r[0] : -1.0;
 }
 
 double msm_measure_madd_rate(void *context, int32_t iters) {
@@ -1353,6 +1479,7 @@ __global__ void k_noalloc_plan(JobDesc jd, uint32_t red_log2, JobDesc *jobs, Win
   if (w >= jd.nwin) return;
   const uint32_t L = 1u << red_log2;
   const uint32_t nseg_low = (jd.nb + L - 1) / L;
+  const uint32_t ngrp_low = (nseg_low + 511) / 512;
   WinDesc wd;
   wd.job = 0;
   wd.w = w;
@@ -1360,6 +1487,8 @@ __global__ void k_noalloc_plan(JobDesc jd, uint32_t red_log2, JobDesc *jobs, Win
   wd.nb = (w + 1 == jd.nwin) ? jd.nb_top : jd.nb;
   wd.seg_begin = w * nseg_low;
   wd.nseg = (wd.nb + L - 1) / L;
+  wd.grp_begin = w * ngrp_low;
+  wd.ngrp = (wd.nseg + 511) / 512;
   wins[w] = wd;
 }
 
@@ -1403,12 +1532,15 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   jd.base_off = base_offset;
   jd.c = MSM_NOALLOC_WINDOW_BITS;
   jd.signed_digits = 1;
-  uint32_t nbk = 0, nsegs = 0;
+  uint32_t nbk = 0, nsegs = 0, ngrps = 0;
   const uint32_t L = 1u << MSM_NOALLOC_RED_LOG2;
   if (n) {
     layout(jd.c, 1, jd.nwin, jd.nb, jd.nb_top);
+    jd.nred = jd.nwin;
     nbk = (jd.nwin - 1) * jd.nb + jd.nb_top;
-    nsegs = (jd.nwin - 1) * ((jd.nb + L - 1) / L) + (jd.nb_top + L - 1) / L;
+    const uint32_t nseg_low = (jd.nb + L - 1) / L, nseg_top = (jd.nb_top + L - 1) / L;
+    nsegs = (jd.nwin - 1) * nseg_low + nseg_top;
+    ngrps = (jd.nwin - 1) * ((nseg_low + 511) / 512) + (nseg_top + 511) / 512;
   }
   const uint64_t entries = n * jd.nwin;
   const uint32_t tasks = (uint32_t)(nbk + entries / MSM_NOALLOC_SEG_LEN + 1);
@@ -1423,7 +1555,10 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   const size_t o_vals = carve(off, entries * 4);
   const size_t o_tasks = carve(off, (size_t)tasks * sizeof(Task));
   const size_t o_part = carve(off, (size_t)tasks * MSM_BUCKET_BYTES);
+  const size_t o_order = carve(off, (size_t)tasks * 4);
+  const size_t o_lenh = carve(off, (size_t)(MSM_NOALLOC_SEG_LEN + 1) * 4);
   const size_t o_seg = carve(off, (size_t)nsegs * 2 * MSM_BUCKET_BYTES);
+  const size_t o_grp = carve(off, (size_t)ngrps * 2 * MSM_BUCKET_BYTES);
   const size_t o_win = carve(off, (size_t)jd.nwin * MSM_BUCKET_BYTES);
   if (off > MSM_NOALLOC_SCRATCH_BYTES)
     return fail(ERR_BUDGET, "msm_mult_noalloc: scratch layout needs %zu bytes", off);
@@ -1436,7 +1571,7 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   pb.class_pts = cx->class_pts.as<uint4>();
   pb.n_special = cx->n_special;
   pb.n_classes = cx->n_classes;
-  pb.n_bases = cx->npoints;
+  pb.n_bases = cx->npoints * cx->fb_w;
   pb.scalars = (const uint4 *)d_scalars;
   pb.jobs = (const JobDesc *)(s + o_jobs);
   pb.wins = (const WinDesc *)(s + o_wins);
@@ -1445,8 +1580,10 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   pb.n_points = n;
   pb.n_buckets = nbk;
   pb.n_segs = nsegs;
+  pb.n_grps = ngrps;
   pb.seg_len = MSM_NOALLOC_SEG_LEN;
   pb.red_len_log2 = MSM_NOALLOC_RED_LOG2;
+  pb.grp_len_log2 = 9;
   pb.max_entries = entries;
   pb.max_tasks = tasks;
   pb.count = (uint32_t *)(s + o_count);
@@ -1459,7 +1596,10 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   pb.vals = (uint32_t *)(s + o_vals);
   pb.tasks = (Task *)(s + o_tasks);
   pb.partials = (uint4 *)(s + o_part);
+  pb.order = (uint32_t *)(s + o_order);
+  pb.len_hist = (uint32_t *)(s + o_lenh);
   pb.seg_out = (uint4 *)(s + o_seg);
+  pb.grp_out = (uint4 *)(s + o_grp);
   pb.win_sum = (uint4 *)(s + o_win);
   pb.results = (uint64_t *)d_out;
   cudaStream_t st = (cudaStream_t)stream;

@@ -6,8 +6,8 @@
 //   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
 //   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
 //   6. k_merge     buckets split over several runs: warp-parallel sum of their partials
-//   7. k_reduce1   per window segment: running sum R and triangle sum A (pippenger.h:25-33)
-//   8. k_reduce2   per window: combine segments -> window sum
+//   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33)
+//   8. k_reduce2/3 combine runs into groups, groups into window sums
 //   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
 //                  Weierstrass, add the bases without a twisted-Edwards image
 //                  (driver.cpp:349-372), write g1_projective_t (bls12_377_g1.h:427-439, 667-690)
@@ -74,8 +74,10 @@ __device__ __forceinline__ int32_t window_digit(const ScalarBits &s, const JobDe
   return d;
 }
 
+// Global bucket id of digit magnitude `mag` in window w.  Fixed-base jobs keep one bucket array
+// for all windows: their entries point at the window's own table of 2^(c w) P_i instead.
 __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, uint32_t mag) {
-  return jd.bucket_begin + w * jd.nb + (mag - 1u);
+  return jd.bucket_begin + (jd.fixed ? 0u : w * jd.nb) + (mag - 1u);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -238,8 +240,9 @@ __global__ void k_scatter(PassBuffers pb) {
     basepos = __shfl_sync(peers, basepos, leader);
     const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
     const uint64_t pos = (uint64_t)pb.offset[key] + basepos + rank;
+    const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
     if (pos < pb.max_entries) {
-      pb.vals[pos] = (uint32_t)bidx | (d < 0 ? 0x80000000u : 0u);
+      pb.vals[pos] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
     } else {
       set_error(pb.counters, 3, (uint32_t)pos);
     }
@@ -247,8 +250,37 @@ __global__ void k_scatter(PassBuffers pb) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// 4. tasks
+// 4. tasks: runs of <= seg_len entries, and a processing order with the longest runs first.
+//    Lanes of one warp then get runs of (almost) equal length, so no lane idles while another
+//    finishes a longer bucket; long runs also start first, which evens out the tail.
 // ---------------------------------------------------------------------------------------------
+__global__ void k_len_hist(PassBuffers pb) {
+  extern __shared__ uint32_t h[];
+  for (uint32_t i = threadIdx.x; i <= pb.seg_len; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < pb.n_buckets; b += gridDim.x * blockDim.x) {
+    const uint32_t cnt = pb.count[b];
+    if (!cnt) continue;
+    const uint32_t nt = ntask_of(cnt, pb.seg_len);
+    atomicAdd(&h[cnt - (nt - 1) * pb.seg_len], 1u);
+    if (nt > 1) atomicAdd(&h[pb.seg_len], nt - 1);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i <= pb.seg_len; i += blockDim.x)
+    if (h[i]) atomicAdd(&pb.len_hist[i], h[i]);
+}
+
+// cursor[len] = number of tasks longer than len (longest first); one thread, seg_len + 1 bins
+__global__ void k_len_scan(PassBuffers pb) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint32_t acc = 0;
+  for (uint32_t l = pb.seg_len + 1; l-- > 0;) {
+    const uint32_t c = pb.len_hist[l];
+    pb.len_hist[l] = acc;
+    acc += c;
+  }
+}
+
 __global__ void k_tasks(PassBuffers pb) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= pb.n_buckets) return;
@@ -258,23 +290,40 @@ __global__ void k_tasks(PassBuffers pb) {
   const uint32_t nt = ntask_of(cnt, pb.seg_len);
   const uint32_t t0 = pb.taskoff[b];
   const uint32_t off = pb.offset[b];
+  if (t0 + nt > pb.max_tasks) {
+    set_error(pb.counters, 4, t0 + nt);
+    return;
+  }
   for (uint32_t k = 0; k < nt; k++) {
-    const uint32_t t = t0 + k;
-    if (t >= pb.max_tasks) { set_error(pb.counters, 4, t); return; }
     Task tk;
     tk.start = off + k * pb.seg_len;
     tk.len = min(pb.seg_len, cnt - k * pb.seg_len);
     tk.bucket = b;
     tk.pad = 0;
-    pb.tasks[t] = tk;
+    pb.tasks[t0 + k] = tk;
   }
-  if (nt > 1) pb.heavy[atomicAdd(&pb.counters[CNT_HEAVY], 1u)] = b;
+  // processing order: full runs reserve a block of slots in the seg_len bin, the last run one
+  // slot in the bin of its length (warp-aggregated)
+  if (nt > 1) {
+    const uint32_t base = atomicAdd(&pb.len_hist[pb.seg_len], nt - 1);
+    for (uint32_t k = 0; k + 1 < nt; k++) pb.order[base + k] = t0 + k;
+    pb.heavy[atomicAdd(&pb.counters[CNT_HEAVY], 1u)] = b;
+  }
+  const uint32_t last = cnt - (nt - 1) * pb.seg_len;
+  const uint32_t active = __activemask();
+  const uint32_t peers = __match_any_sync(active, last);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  uint32_t pos = 0;
+  if (lane == leader) pos = atomicAdd(&pb.len_hist[last], (uint32_t)__popc(peers));
+  pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+  pb.order[pos] = t0 + nt - 1;
 }
 
 // ---------------------------------------------------------------------------------------------
 // 5. bucket accumulation (persistent; warps fetch 32 tasks at a time)
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_accumulate(PassBuffers pb) {
+__global__ void __launch_bounds__(128, 4) k_accumulate(PassBuffers pb) {
   const int lane = threadIdx.x & 31;
   const uint32_t ntasks = pb.counters[CNT_TASKS];
   if (pb.counters[CNT_ERROR]) return;
@@ -283,8 +332,9 @@ __global__ void __launch_bounds__(256) k_accumulate(PassBuffers pb) {
     if (lane == 0) first = atomicAdd(&pb.counters[CNT_TASK_CURSOR], 32u);
     first = __shfl_sync(0xffffffffu, first, 0);
     if (first >= ntasks) break;
-    const uint32_t t = first + lane;
-    if (t < ntasks) {
+    const uint32_t i = first + lane;
+    if (i < ntasks) {
+      const uint32_t t = pb.order[i];
       const Task tk = pb.tasks[t];
       xyzt_t acc = xyzt_identity();
       for (uint32_t e = 0; e < tk.len; e++) {
@@ -351,14 +401,28 @@ __global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// 7. level-1 reduction: per segment of 2^red_len_log2 buckets, from the top bucket down,
-//    running R += B_b and A += R (triangleSumUpdate, pippenger.h:25-33)
+// 7-8. bucket reduction: window sum = sum_b (b + 1) B_b over the window's buckets (digit
+//    magnitude b + 1), the triangle sum of pippenger.h:25-33 computed in three parallel levels.
+//    A run of items summarised as (R, A) -- R = sum of the items' point sums, A = sum of
+//    (local position + 1) * point -- combines exactly: a run of runs has
+//    A = sum_i A_i + len * sum_i i R_i, and len is a power of two (doublings only).
+//    level 1: runs of 2^red_len_log2 buckets, one thread each (throughput part);
+//    level 2: groups of 2^grp_len_log2 level-1 runs, one block each;
+//    level 3: the groups of one window, one block per window.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t find_win(const WinDesc *wins, uint32_t n_wins, uint32_t s) {
   uint32_t lo = 0, hi = n_wins;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
     if (wins[mid].seg_begin <= s) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ uint32_t find_win_grp(const WinDesc *wins, uint32_t n_wins, uint32_t g) {
+  uint32_t lo = 0, hi = n_wins;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (wins[mid].grp_begin <= g) lo = mid; else hi = mid;
   }
   return lo;
 }
@@ -373,16 +437,17 @@ __global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
   const uint32_t hi = min(lo + L, wd.nb);
   xyzt_t R = xyzt_identity(), A = xyzt_identity();
   bool r_live = false, a_live = false;
+#pragma unroll 1
   for (uint32_t b = hi; b-- > lo;) {
     const uint32_t gb = wd.bucket_begin + b;
     if (pb.count[gb] != 0) {
       xyzt_t B;
       xyzt_load(B, pb.partials + (size_t)pb.taskoff[gb] * 12);
-      R = r_live ? te_add_ool(R, B) : B;
+      R = r_live ? te_add(R, B) : B;
       r_live = true;
     }
     if (r_live) {
-      A = a_live ? te_add_ool(A, R) : R;
+      A = a_live ? te_add(A, R) : R;
       a_live = true;
     }
   }
@@ -390,44 +455,15 @@ __global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
   xyzt_store(pb.seg_out + (size_t)s * 24 + 12, A);
 }
 
-// ---------------------------------------------------------------------------------------------
-// 8. level-2 reduction: one block per window.  Window sum = sum_s A_s + L * sum_s s * R_s;
-//    thread t takes a contiguous run of segments starting at s0 and contributes
-//    SA + L * (T + s0 * RR) with SA = sum A_s, RR = sum R_s, T = sum (s - s0) R_s; the block
-//    then sums the contributions in a shared-memory tree.
-// ---------------------------------------------------------------------------------------------
-constexpr int kRed2Threads = 128;
+constexpr int kRedThreads = 128;
 
-__global__ void __launch_bounds__(kRed2Threads) k_reduce2(PassBuffers pb) {
-  if (pb.counters[CNT_ERROR]) return;
-  const uint32_t gw = blockIdx.x;
-  if (gw >= pb.n_wins) return;
-  __shared__ uint4 sh[kRed2Threads * 12];
-  const WinDesc wd = pb.wins[gw];
+// Sum of a block's points in shared memory; the result is valid in thread 0.
+__device__ __forceinline__ xyzt_t block_sum(xyzt_t X, uint4 *sh) {
   const uint32_t tid = threadIdx.x;
-  const uint32_t per = (wd.nseg + kRed2Threads - 1) / kRed2Threads;
-  const uint32_t s0 = tid * per;
-  const uint32_t s1 = min(s0 + per, wd.nseg);
-  xyzt_t X = xyzt_identity();
-  if (s0 < s1) {
-    xyzt_t SA = xyzt_identity(), T = xyzt_identity(), RR = xyzt_identity();
-    for (uint32_t s = s1; s-- > s0;) {
-      T = te_add_ool(T, RR);
-      xyzt_t R, A;
-      xyzt_load(R, pb.seg_out + (size_t)(wd.seg_begin + s) * 24);
-      xyzt_load(A, pb.seg_out + (size_t)(wd.seg_begin + s) * 24 + 12);
-      RR = te_add_ool(RR, R);
-      SA = te_add_ool(SA, A);
-    }
-    X = s0 > 0 ? te_add_ool(T, te_mul_small(RR, s0)) : T;
-#pragma unroll 1
-    for (uint32_t k = 0; k < pb.red_len_log2; k++) X = te_dbl_ool(X);
-    X = te_add_ool(X, SA);
-  }
   xyzt_store(sh + tid * 12, X);
   __syncthreads();
 #pragma unroll 1
-  for (uint32_t stride = kRed2Threads / 2; stride > 0; stride >>= 1) {
+  for (uint32_t stride = kRedThreads / 2; stride > 0; stride >>= 1) {
     if (tid < stride) {
       xyzt_t o;
       xyzt_load(o, sh + (tid + stride) * 12);
@@ -436,7 +472,97 @@ __global__ void __launch_bounds__(kRed2Threads) k_reduce2(PassBuffers pb) {
     }
     __syncthreads();
   }
-  if (tid == 0) xyzt_store(pb.win_sum + (size_t)gw * 12, X);
+  return X;
+}
+
+// Inclusive suffix sums over the block: thread t gets sum_{u >= t} X_u (Hillis-Steele).
+__device__ __forceinline__ xyzt_t block_suffix_scan(xyzt_t X, uint4 *sh) {
+  const uint32_t tid = threadIdx.x;
+  xyzt_store(sh + tid * 12, X);
+  __syncthreads();
+#pragma unroll 1
+  for (uint32_t d = 1; d < kRedThreads; d <<= 1) {
+    xyzt_t o;
+    const bool has = tid + d < kRedThreads;
+    if (has) xyzt_load(o, sh + (tid + d) * 12);
+    __syncthreads();
+    if (has) {
+      X = te_add_ool(X, o);
+      xyzt_store(sh + tid * 12, X);
+    }
+    __syncthreads();
+  }
+  return X;
+}
+
+// Combine `cnt` runs (R, A) of 2^lin_log2 buckets each into one run (result in thread 0).
+// Thread t takes runs [t per, t per + per) (per a power of two) and forms SA = sum A_i,
+// RR = sum R_i and T = sum (i - t per) R_i.  Then
+//   A = sum_t SA_t + 2^lin_log2 (sum_t T_t + per sum_t t RR_t),  R = sum_t RR_t,
+// where sum_t t RR_t = sum_{t >= 1} (suffix sum of RR at t): one block scan and three block
+// sums, and only thread 0 doubles.
+__device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log2, bool want_r,
+                              uint4 *sh, xyzt_t &A_out, xyzt_t &R_out) {
+  const uint32_t tid = threadIdx.x;
+  uint32_t per = 1, per_log2 = 0;
+  while (per * kRedThreads < cnt) {
+    per <<= 1;
+    per_log2++;
+  }
+  const uint32_t i0 = tid * per, i1 = min(i0 + per, cnt);
+  xyzt_t SA = xyzt_identity(), T = xyzt_identity(), RR = xyzt_identity();
+#pragma unroll 1
+  for (uint32_t i = i1; i-- > i0;) {
+    T = te_add_ool(T, RR);
+    xyzt_t R, A;
+    xyzt_load(R, items + (size_t)i * 24);
+    xyzt_load(A, items + (size_t)i * 24 + 12);
+    RR = te_add_ool(RR, R);
+    SA = te_add_ool(SA, A);
+  }
+  const xyzt_t suf = block_suffix_scan(RR, sh);
+  if (want_r && tid == 0) R_out = suf;  // suffix at 0 is the total
+  const xyzt_t sumY = block_sum(tid ? suf : xyzt_identity(), sh);
+  const xyzt_t sumT = block_sum(T, sh);
+  const xyzt_t sumSA = block_sum(SA, sh);
+  if (tid == 0) {
+    xyzt_t X = sumY;
+#pragma unroll 1
+    for (uint32_t k = 0; k < per_log2; k++) X = te_dbl_ool(X);
+    X = te_add_ool(sumT, X);
+#pragma unroll 1
+    for (uint32_t k = 0; k < lin_log2; k++) X = te_dbl_ool(X);
+    A_out = te_add_ool(X, sumSA);
+  }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_reduce2(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t g = blockIdx.x;
+  if (g >= pb.n_grps) return;
+  __shared__ uint4 sh[kRedThreads * 12];
+  const WinDesc wd = pb.wins[find_win_grp(pb.wins, pb.n_wins, g)];
+  const uint32_t G = 1u << pb.grp_len_log2;
+  const uint32_t first = (g - wd.grp_begin) * G;
+  const uint32_t cnt = min(G, wd.nseg - first);
+  xyzt_t A, R;
+  block_combine(pb.seg_out + (size_t)(wd.seg_begin + first) * 24, cnt, pb.red_len_log2, true, sh, A, R);
+  if (threadIdx.x == 0) {
+    xyzt_store(pb.grp_out + (size_t)g * 24, R);
+    xyzt_store(pb.grp_out + (size_t)g * 24 + 12, A);
+  }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t gw = blockIdx.x;
+  if (gw >= pb.n_wins) return;
+  __shared__ uint4 sh[kRedThreads * 12];
+  const WinDesc wd = pb.wins[gw];
+  xyzt_t A, R;
+  block_combine(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp, pb.red_len_log2 + pb.grp_len_log2,
+                false, sh, A, R);
+  if (threadIdx.x == 0) xyzt_store(pb.win_sum + (size_t)gw * 12, A);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -446,6 +572,61 @@ __device__ __forceinline__ void load_class_point(wpt_t &p, const uint4 *cp) {
   fq_load(p.x, cp);
   fq_load(p.y, cp + 3);
   p.z = fq_one();
+}
+
+// ---- 4-lane cooperative point operations for the serial window combine ----
+// Lanes 0..3 (mask 0xf) hold the same point.  Each lane computes one of four independent
+// products and the lanes swap results, so a doubling costs two product latencies instead of
+// eight, and an addition three instead of nine.
+__device__ __forceinline__ fq_t shfl4(const fq_t &a, int src) {
+  fq_t r;
+#pragma unroll
+  for (int k = 0; k < FQ_LIMBS; k++) r.v[k] = __shfl_sync(0xfu, a.v[k], src, 4);
+  return r;
+}
+__device__ __forceinline__ fq_t pick4(int l, const fq_t &a, const fq_t &b, const fq_t &c, const fq_t &d) {
+  return fq_select(l == 0, a, fq_select(l == 1, b, fq_select(l == 2, c, d)));
+}
+
+__device__ __noinline__ xyzt_t te_dbl_quad(const xyzt_t &p) {
+  const int l = threadIdx.x & 3;
+  const fq_t sq = fq_sqr(pick4(l, p.x, p.y, p.z, fq_add(p.x, p.y)));
+  const fq_t A = shfl4(sq, 0), B = shfl4(sq, 1), ZZ = shfl4(sq, 2), S = shfl4(sq, 3);
+  const fq_t C = fq_dbl(ZZ);
+  const fq_t D = fq_neg(A);
+  const fq_t E = fq_sub(fq_sub(S, A), B);
+  const fq_t G = fq_add(D, B);
+  const fq_t F = fq_sub(G, C);
+  const fq_t H = fq_sub(D, B);
+  const fq_t pr = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
+  xyzt_t r;
+  r.x = shfl4(pr, 0);
+  r.y = shfl4(pr, 1);
+  r.t = shfl4(pr, 2);
+  r.z = shfl4(pr, 3);
+  return r;
+}
+
+__device__ __noinline__ xyzt_t te_add_quad(const xyzt_t &p, const xyzt_t &q) {
+  const uint32_t kc[FQ_LIMBS] = BLS_TE_K;
+  const int l = threadIdx.x & 3;
+  const fq_t m1 = pick4(l, fq_sub(p.y, p.x), fq_add(p.y, p.x), p.t, p.z);
+  const fq_t m2 = pick4(l, fq_sub(q.y, q.x), fq_add(q.y, q.x), q.t, q.z);
+  const fq_t pr = fq_mul(m1, m2);
+  const fq_t A = shfl4(pr, 0), B = shfl4(pr, 1), TT = shfl4(pr, 2), ZZ = shfl4(pr, 3);
+  const fq_t C = fq_mul(TT, fq_from(kc));
+  const fq_t D = fq_dbl(ZZ);
+  const fq_t E = fq_sub(B, A);
+  const fq_t F = fq_sub(D, C);
+  const fq_t G = fq_add(D, C);
+  const fq_t H = fq_add(B, A);
+  const fq_t pr2 = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
+  xyzt_t r;
+  r.x = shfl4(pr2, 0);
+  r.y = shfl4(pr2, 1);
+  r.t = shfl4(pr2, 2);
+  r.z = shfl4(pr2, 3);
+  return r;
 }
 
 __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
@@ -464,38 +645,43 @@ __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
     atomicAdd(&cls_sum[pb.special_cls[s] & 7], w0.x & 3u);
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x >= 4) return;  // lanes 0..3 of warp 0 run the combine together
   uint64_t *out = pb.results + (size_t)jd.result_slot * 18;
   if (pb.counters[CNT_ERROR]) {
-    for (int k = 0; k < 18; k++) out[k] = 0;
+    if (threadIdx.x == 0)
+      for (int k = 0; k < 18; k++) out[k] = 0;
     return;
   }
+  // Horner over the windows: acc = 2^c * acc + WS_w (pippenger.h:36-45 doubles per offset)
   xyzt_t acc = xyzt_identity();
-  if (jd.n > 0 && jd.nwin > 0) {
-    xyzt_load(acc, pb.win_sum + (size_t)(jd.win_begin + jd.nwin - 1) * 12);
+  if (jd.n > 0 && jd.nred > 0) {
+    xyzt_load(acc, pb.win_sum + (size_t)(jd.win_begin + jd.nred - 1) * 12);
 #pragma unroll 1
-    for (int w = (int)jd.nwin - 2; w >= 0; w--) {
+    for (int w = (int)jd.nred - 2; w >= 0; w--) {
 #pragma unroll 1
-      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_ool(acc);
+      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_quad(acc);
       xyzt_t ws;
       xyzt_load(ws, pb.win_sum + (size_t)(jd.win_begin + w) * 12);
-      acc = te_add_ool(acc, ws);
+      acc = te_add_quad(acc, ws);
     }
   }
-  wpt_t res = te_to_weierstrass(acc);
+  if (threadIdx.x != 0) return;
+  wpt_t res = te_to_weierstrass(acc);  // z is 1, or 0 for infinity
+  bool added = false;
   for (uint32_t c = 0; c < pb.n_classes && c < 8; c++) {
     const uint32_t m = cls_sum[c] & 3u;
     if (m == 0) continue;
     wpt_t p;
     load_class_point(p, pb.class_pts + c * 6);
     for (uint32_t k = 0; k < m; k++) res = w_add(res, p);
+    added = true;
   }
-  res = w_normalize(res);
+  if (added) res = w_normalize(res);
   // g1_projective_t {x[6], y[6], z[6]}: (x*R, y*R, R) or arkworks' zero() (R, R, 0)
   const fq_t one = fq_canon(fq_one());
   const bool inf = fq_is_zero(res.z);
-  const fq_t ox = inf ? one : res.x;
-  const fq_t oy = inf ? one : res.y;
+  const fq_t ox = inf ? one : fq_canon(res.x);
+  const fq_t oy = inf ? one : fq_canon(res.y);
   const fq_t oz = inf ? fq_zero() : one;
   for (int k = 0; k < 6; k++) {
     out[k] = ((uint64_t)ox.v[2 * k + 1] << 32) | ox.v[2 * k];
@@ -518,6 +704,7 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   if ((e = cudaMemsetAsync(pb.count, 0, (size_t)pb.n_buckets * 4, st))) return e;
   if ((e = cudaMemsetAsync(pb.fill, 0, (size_t)pb.n_buckets * 4, st))) return e;
   if ((e = cudaMemsetAsync(pb.counters, 0, CNT_WORDS * 4, st))) return e;
+  if ((e = cudaMemsetAsync(pb.len_hist, 0, (size_t)(pb.seg_len + 1) * 4, st))) return e;
   mark(0);
   const uint32_t pts_blocks = (uint32_t)((pb.n_points + 255) / 256);
   if (pb.n_points > 0) k_count<<<pts_blocks, 256, 0, st>>>(pb);
@@ -531,17 +718,23 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   mark(2);
   if (pb.n_points > 0) k_scatter<<<pts_blocks, 256, 0, st>>>(pb);
   mark(3);
-  if (pb.n_buckets > 0) k_tasks<<<(pb.n_buckets + 255) / 256, 256, 0, st>>>(pb);
+  if (pb.n_buckets > 0) {
+    k_len_hist<<<num_sms * 4, 256, (pb.seg_len + 1) * 4, st>>>(pb);
+    k_len_scan<<<1, 32, 0, st>>>(pb);
+    k_tasks<<<(pb.n_buckets + 255) / 256, 256, 0, st>>>(pb);
+  }
   mark(4);
-  k_accumulate<<<num_sms * 2, 256, 0, st>>>(pb);
+  k_accumulate<<<num_sms * 4, 128, 0, st>>>(pb);
   mark(5);
   k_merge<<<num_sms, 256, 0, st>>>(pb);
   mark(6);
   if (pb.n_segs > 0) k_reduce1<<<(pb.n_segs + 127) / 128, 128, 0, st>>>(pb);
   mark(7);
-  if (pb.n_wins > 0) k_reduce2<<<pb.n_wins, kRed2Threads, 0, st>>>(pb);
+  if (pb.n_grps > 0) k_reduce2<<<pb.n_grps, kRedThreads, 0, st>>>(pb);
   mark(8);
-  if (pb.n_jobs > 0) k_final<<<pb.n_jobs, 128, 0, st>>>(pb);
+  if (pb.n_wins > 0) k_reduce3<<<pb.n_wins, kRedThreads, 0, st>>>(pb);
   mark(9);
+  if (pb.n_jobs > 0) k_final<<<pb.n_jobs, 128, 0, st>>>(pb);
+  mark(10);
   return cudaGetLastError();
 }

@@ -52,6 +52,8 @@ typedef struct {
  * ------------------------------------------------------------------------------------------- */
 
 /* Load the bases once and keep them resident on the GPU in precomputed twisted-Edwards form.
+ * For 2^20 bases or more, when HBM allows, it also keeps fixed-base tables 2^(c w) P_i for every
+ * window w (environment: MSM_FIXED_BASE=0 off, =<c> force width c; MSM_FIXED_BASE_MAX_GB).
  * Replaces `extern "C" Driver *msm_init(const char *xclbin, ssize_t xclbin_len,
  * g1_affine_t *rust_points, ssize_t npoints)` (zprize/msm_pippenger/host/driver/driver.cpp:603-617).
  * `xclbin` names an FPGA bitstream in the reference; here it is accepted and ignored (it may be
@@ -78,6 +80,7 @@ typedef struct {
   int32_t red_len_log2;  /* log2 of buckets per level-1 reduction segment */
   int32_t use_graph;     /* 1 replay the pass from a captured CUDA graph, 2 never, 0 auto */
   int32_t mode;          /* msm_mult: 1 one pass per MSM (default), 2 all MSMs in one pass */
+  int32_t fixed_base;    /* 1 use the context's fixed-base tables, 2 never, 0 auto (cost model) */
 } msm_options_t;
 
 /* Error code of the last failed call on this thread (0 if none) and its message. */
@@ -112,7 +115,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
 
 /* Per-stage device times (ms, CUDA events on the pipeline stream) of the last pass when timing
  * is enabled with msm_set_timing(ctx, 1). Stage order: count, scan, scatter, tasks, accumulate,
- * merge, reduce1, reduce2, final. Returns the number of stages written. */
+ * merge, reduce1, reduce2, reduce3, final. Returns the number of stages written. */
 int msm_set_timing(void *context, int32_t enable);
 int msm_last_timings(void *context, double *ms, int32_t max_stages);
 /* Counters of the last pass: tasks, heavy buckets, sorted entries, buckets. */
@@ -159,11 +162,16 @@ int msm_generate_bases(uint64_t seed, uint64_t first, uint64_t n, g1_affine_t *o
  * 10% 16-bit, 10% 0 or r-1, 10% one repeated value), drawn for MSM `msm_index`. */
 int msm_generate_scalars(uint64_t seed, uint64_t n, int32_t kind, uint64_t msm_index,
                          biginteger256_t *out);
-/* Measured peak rate of the GPU's IMAD pipe (32-bit multiply-adds per second, all SMs). */
+/* Measured peak rate of the GPU's IMAD pipe on independent mad.lo/mad.hi pairs (32-bit
+ * multiply-adds per second, all SMs, after a warm-up). `iters` is ignored. */
 double msm_measure_imad_peak(int32_t iters);
+/* The same for up to three instruction mixes: rates[0] mad.lo/mad.hi pairs, rates[1] mad.lo
+ * only, rates[2] mad.hi only.  Returns the number of rates written. */
+int msm_measure_int_peaks(double *rates, int32_t n);
 /* Device name, SM count and clock as text. */
 int msm_device_info(char *buf, size_t len);
-/* Field self-test: op 0 mul (Montgomery), 1 add, 2 sub, 3 inverse, 4 canonicalise, 5 negate;
+/* Field self-test: op 0 mul (Montgomery), 1 add, 2 sub, 3 inverse (Fermat), 4 canonicalise,
+ * 5 negate, 6 inverse (binary extended Euclid);
  * operands are 12 little-endian u32 limbs each. */
 int msm_field_selftest(int32_t op, const uint32_t *a, const uint32_t *b, uint32_t *out, uint64_t n);
 /* Throughput of the mixed twisted-Edwards addition on cached bases (adds per second). */

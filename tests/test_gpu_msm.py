@@ -58,6 +58,7 @@ def test_field_ops(engine, ref):
     can = engine.field_selftest(4, a, b)
     neg = engine.field_selftest(5, a, b)
     inv = engine.field_selftest(3, a, b)
+    inv_bgcd = engine.field_selftest(6, a, b)
     for i, (x, y) in enumerate(zip(vals, other)):
         m = from32(mul[i])
         assert m < 2 * Q and m % Q == x * y * Rinv % Q
@@ -69,11 +70,12 @@ def test_field_ops(engine, ref):
         assert c < Q and c == x % Q
         ng = from32(neg[i])
         assert ng < 2 * Q and ng % Q == (-x) % Q
-        iv = from32(inv[i])
-        if x % Q:
-            assert iv % Q * x % Q == R * R % Q
-        else:
-            assert iv % Q == 0
+        for arr in (inv, inv_bgcd):
+            iv = from32(arr[i])
+            if x % Q:
+                assert iv % Q * x % Q == R * R % Q
+            else:
+                assert iv % Q == 0
 
 
 # ---- generator -------------------------------------------------------------------------------
@@ -299,3 +301,64 @@ def test_msm_2_18_against_oracle(engine, ocpu):
     sc = engine.generate_scalars(2, n)
     out = msm_gpu(engine, pts, sc)
     assert np.array_equal(out[0], ocpu.msm(pts, sc))
+
+
+# ---- fixed-base tables (2^(c w) P_i per window, one shared bucket array) ----------------------
+def _ctx_with_fixed_base(engine, pts, c):
+    import os
+    old = os.environ.get("MSM_FIXED_BASE")
+    os.environ["MSM_FIXED_BASE"] = str(c)
+    try:
+        return engine.multi_scalar_mult_init(pts)
+    finally:
+        if old is None:
+            del os.environ["MSM_FIXED_BASE"]
+        else:
+            os.environ["MSM_FIXED_BASE"] = old
+
+
+def test_fixed_base_parity(engine, ref, ocpu, kats):
+    nb = 3000
+    pts = ocpu.gen_bases(4321, nb)
+    sp = special_points(ref, kats)
+    pts[17] = np.frombuffer(ref.encode_affine(sp[0]), dtype=np.uint8)   # order-4 point, no TE image
+    pts[18] = np.frombuffer(ref.encode_affine(ref.INF), dtype=np.uint8)
+    ctx = _ctx_with_fixed_base(engine, pts, 13)
+    try:
+        assert ctx.config(nb)["fixed_base"] in (1, 2)
+        sc = engine.generate_scalars(4322, 2 * nb)
+        for opts in (dict(fixed_base=1), dict(fixed_base=1, mode=2), dict(fixed_base=1, seg_len=8),
+                     dict(fixed_base=2)):
+            out = ctx.mult(sc, **opts)
+            for b in range(2):
+                assert np.array_equal(out[b], ocpu.msm(pts, sc[b * nb:(b + 1) * nb])), (opts, b)
+        sizes = [1, 700, 0, 2999, 64]
+        offs = [2999, 5, 0, 1, 2000]
+        usc = np.concatenate([engine.generate_scalars(77 + j, s, kind=1, msm_index=j) for j, s in enumerate(sizes)])
+        first = np.concatenate([[0], np.cumsum(sizes)])
+        for opts in (dict(fixed_base=1, mode=2), dict(fixed_base=1, mode=2, use_graph=1), dict(mode=2)):
+            out = ctx.mult_uneven(sizes, offs, usc, **opts)
+            for j, (s, o) in enumerate(zip(sizes, offs)):
+                assert np.array_equal(out[j], ocpu.msm(pts[o:o + s], usc[first[j]:first[j] + s])), (opts, j)
+    finally:
+        ctx.close()
+
+
+def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
+    """The reference's second edge case holds a representable base of order 4, whose doubling
+    chain reaches the order-two point (0, -1) and then the identity; the tables stay exact.  (A
+    chain that left the affine curve would switch the context to the plain table.)"""
+    sp = special_points(ref, kats)
+    pts_l = [sp[0], sp[2], ref.neg(ref.add(sp[0], sp[2])), sp[2]] + [ref.mul(ref.GEN, k + 2) for k in range(60)]
+    P = recs(ref, pts_l)
+    ctx = _ctx_with_fixed_base(engine, P, 13)
+    try:
+        ks = [1] * 4 + [k * 977 + 5 for k in range(60)]
+        for fb in (1, 2):
+            out = ctx.mult(scal(ref, ks), fixed_base=fb)
+            assert ref.decode_projective(out[0].tobytes()) == ref.msm_naive(pts_l, ks), fb
+        ks2 = [3, 7, 5, 2] + [(k * 7919) ** 3 % ref.R_SCALAR for k in range(60)]
+        out = ctx.mult(scal(ref, ks2), fixed_base=1)
+        assert ref.decode_projective(out[0].tobytes()) == ref.msm_naive(pts_l, ks2)
+    finally:
+        ctx.close()
