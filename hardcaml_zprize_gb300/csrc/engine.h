@@ -112,8 +112,11 @@ struct PassBuffers {
 
 // launch the whole pipeline of one pass on `stream` (graph-capturable: fixed launch shapes)
 // `stage_events` (10 events, or null) are recorded around the stages for per-kernel timing
+// `chunk_ready` (nchunks events, or null): the scalars arrive in nchunks equal point ranges and
+// the histogram of range c waits for event c (copy/compute overlap for host-resident scalars)
 cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t stream,
-                            cudaEvent_t *stage_events);
+                            cudaEvent_t *stage_events, const cudaEvent_t *chunk_ready = nullptr,
+                            int nchunks = 0);
 #define MSM_NUM_STAGES 10
 size_t msm_scan_tmp_words(uint32_t n_buckets);
 

@@ -369,6 +369,8 @@ struct Ctx {
   uint32_t n_special = 0, n_classes = 0;
   cudaStream_t stream = nullptr, copy_stream = nullptr;
   cudaEvent_t copied[2] = {}, freed[2] = {};
+  static constexpr int kCopyChunks = 4;
+  cudaEvent_t chunk_ev[2][kCopyChunks] = {};
   Workspace ws;
   std::mutex mu;
   bool timing = false;
@@ -381,6 +383,8 @@ struct Ctx {
     for (int i = 0; i < 2; i++) {
       if (copied[i]) cudaEventDestroy(copied[i]);
       if (freed[i]) cudaEventDestroy(freed[i]);
+      for (auto &e : chunk_ev[i])
+        if (e) cudaEventDestroy(e);
     }
   }
 };
@@ -431,7 +435,8 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
 // Enqueue one pass on `st`: upload the plan, run the pipeline (directly or from a captured
 // graph), copy the results to ws.res_host + res_offset jobs.  Does not synchronize.
 int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, cudaStream_t st,
-                 bool use_graph, bool timing, size_t res_offset) {
+                 bool use_graph, bool timing, size_t res_offset,
+                 const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0) {
   if (ws.ensure(pl)) return g_err;
   CK(cudaMemcpyAsync(ws.jobs.p, pl.jobs.data(), pl.jobs.size() * sizeof(JobDesc),
                      cudaMemcpyHostToDevice, st));
@@ -443,7 +448,7 @@ int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, 
   if (res_offset * MSM_PROJ_BYTES + pl.jobs.size() * MSM_PROJ_BYTES > ws.res_host.bytes)
     return fail(ERR_STATE, "result staging too small");
   res_dst += res_offset * MSM_PROJ_BYTES;
-  if (use_graph && !timing) {
+  if (use_graph && !timing && !chunk_ready) {
     char tmp[64];
     snprintf(tmp, sizeof(tmp), "#%p#%p", d_scalars, (void *)res_dst);
     const std::string key = pl.key + tmp;
@@ -466,7 +471,7 @@ int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, 
     CK(cudaGraphLaunch(it->second, st));
     return 0;
   }
-  CK(msm_launch_pass(pb, cx->num_sms, st, timing ? ws.ev : nullptr));
+  CK(msm_launch_pass(pb, cx->num_sms, st, timing ? ws.ev : nullptr, chunk_ready, nchunks));
   CK(cudaMemcpyAsync(res_dst, ws.results.p, pl.jobs.size() * MSM_PROJ_BYTES,
                      cudaMemcpyDeviceToHost, st));
   return 0;
@@ -604,17 +609,28 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     Plan pl;
     if (build_plan(one, pl)) return g_err;
     const void *src = d_scalars;
+    const cudaEvent_t *chunks = nullptr;
     if (!src) {
+      // the copy goes up in chunks on the copy stream; each chunk's histogram starts when it lands
       const int slot = (int)(j & 1);
+      const int nch = Ctx::kCopyChunks;
       CK(cudaStreamWaitEvent(cx->copy_stream, cx->freed[slot], 0));
-      if (sizes[j])
-        CK(cudaMemcpyAsync(ws.scalars[slot].p, h_scalars + first[j], sizes[j] * 32,
-                           cudaMemcpyHostToDevice, cx->copy_stream));
-      CK(cudaEventRecord(cx->copied[slot], cx->copy_stream));
-      CK(cudaStreamWaitEvent(cx->stream, cx->copied[slot], 0));
+      const uint64_t per = (sizes[j] + nch - 1) / nch;
+      for (int c = 0; c < nch; c++) {
+        const uint64_t a = std::min<uint64_t>((uint64_t)c * per, sizes[j]);
+        const uint64_t b = std::min<uint64_t>(a + per, sizes[j]);
+        if (b > a)
+          CK(cudaMemcpyAsync((char *)ws.scalars[slot].p + a * 32, h_scalars + first[j] + a,
+                             (b - a) * 32, cudaMemcpyHostToDevice, cx->copy_stream));
+        CK(cudaEventRecord(cx->chunk_ev[slot][c], cx->copy_stream));
+      }
+      // every kernel after the chunked histogram is ordered after the last chunk's event
       src = ws.scalars[slot].p;
+      chunks = cx->chunk_ev[slot];
     }
-    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, j)) return g_err;
+    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, j, chunks,
+                     chunks ? Ctx::kCopyChunks : 0))
+      return g_err;
     if (!d_scalars) CK(cudaEventRecord(cx->freed[(int)(j & 1)], cx->stream));
     if (cx->timing) {
       if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
@@ -644,6 +660,7 @@ int init_device(Ctx *cx) {
     CK(cudaEventCreateWithFlags(&cx->copied[i], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&cx->freed[i], cudaEventDisableTiming));
     CK(cudaEventRecord(cx->freed[i], cx->stream));
+    for (auto &e : cx->chunk_ev[i]) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   return 0;
 }

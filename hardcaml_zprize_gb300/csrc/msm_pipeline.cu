@@ -83,9 +83,9 @@ __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, ui
 // ---------------------------------------------------------------------------------------------
 // 1. histogram
 // ---------------------------------------------------------------------------------------------
-__global__ void k_count(PassBuffers pb) {
-  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= pb.n_points) return;
+__global__ void k_count(PassBuffers pb, uint64_t g_begin, uint64_t g_end) {
+  const uint64_t g = g_begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= g_end || g >= pb.n_points) return;
   const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
   const JobDesc jd = pb.jobs[j];
   const uint64_t i = g - jd.point_begin;
@@ -96,10 +96,16 @@ __global__ void k_count(PassBuffers pb) {
     const int32_t d = window_digit(s, jd, w, carry);
     if (d == 0) continue;
     const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    // a warp whose active lanes all hit one bucket (e.g. equal scalars) adds once; otherwise
+    // every lane adds on its own (distinct buckets for uniform scalars)
     const uint32_t active = __activemask();
-    const uint32_t peers = __match_any_sync(active, key);
-    const int leader = __ffs(peers) - 1;
-    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&pb.count[key], (uint32_t)__popc(peers));
+    const int leader = __ffs(active) - 1;
+    const uint32_t k0 = __shfl_sync(active, key, leader);
+    if (__all_sync(active, key == k0)) {
+      if ((int)(threadIdx.x & 31) == leader) atomicAdd(&pb.count[key], (uint32_t)__popc(active));
+    } else {
+      atomicAdd(&pb.count[key], 1u);
+    }
   }
 }
 
@@ -228,23 +234,55 @@ __global__ void k_scatter(PassBuffers pb) {
   const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
   const int lane = threadIdx.x & 31;
   uint32_t carry = 0;
-  for (uint32_t w = 0; w < jd.nwin; w++) {
-    const int32_t d = window_digit(s, jd, w, carry);
-    if (d == 0) continue;
-    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
-    const uint32_t active = __activemask();
-    const uint32_t peers = __match_any_sync(active, key);
-    const int leader = __ffs(peers) - 1;
-    uint32_t basepos = 0;
-    if (lane == leader) basepos = atomicAdd(&pb.fill[key], (uint32_t)__popc(peers));
-    basepos = __shfl_sync(peers, basepos, leader);
-    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    const uint64_t pos = (uint64_t)pb.offset[key] + basepos + rank;
-    const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
-    if (pos < pb.max_entries) {
-      pb.vals[pos] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
-    } else {
-      set_error(pb.counters, 3, (uint32_t)pos);
+  // four windows per step: their slot atomics and offset loads are independent, so the four
+  // round trips overlap instead of running one after another
+#pragma unroll 1
+  for (uint32_t w0 = 0; w0 < jd.nwin; w0 += 4) {
+    uint32_t key[4], val[4], slot[4], base[4];
+    bool ok[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint32_t w = w0 + k;
+      ok[k] = false;
+      key[k] = 0;
+      val[k] = 0;
+      if (w < jd.nwin) {
+        const int32_t d = window_digit(s, jd, w, carry);
+        if (d != 0) {
+          ok[k] = true;
+          key[k] = bucket_key(jd, w, (uint32_t)abs(d));
+          const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
+          val[k] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      slot[k] = 0;
+      base[k] = 0;
+      if (ok[k]) {
+        const uint32_t active = __activemask();
+        const int leader = __ffs(active) - 1;
+        const uint32_t k0 = __shfl_sync(active, key[k], leader);
+        if (__all_sync(active, key[k] == k0)) {  // one bucket for the whole warp: one atomic
+          uint32_t bp = 0;
+          if (lane == leader) bp = atomicAdd(&pb.fill[key[k]], (uint32_t)__popc(active));
+          slot[k] = __shfl_sync(active, bp, leader) + __popc(active & ((1u << lane) - 1u));
+        } else {
+          slot[k] = atomicAdd(&pb.fill[key[k]], 1u);
+        }
+        base[k] = pb.offset[key[k]];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (!ok[k]) continue;
+      const uint64_t pos = (uint64_t)base[k] + slot[k];
+      if (pos < pb.max_entries) {
+        pb.vals[pos] = val[k];
+      } else {
+        set_error(pb.counters, 3, (uint32_t)pos);
+      }
     }
   }
 }
@@ -696,7 +734,8 @@ size_t msm_scan_tmp_words(uint32_t n_buckets) {
   return 2ull * ((n_buckets + kScanBlock - 1) / kScanBlock) + 2;
 }
 
-cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st, cudaEvent_t *ev) {
+cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st, cudaEvent_t *ev,
+                            const cudaEvent_t *chunk_ready, int nchunks) {
   cudaError_t e;
   auto mark = [&](int k) {
     if (ev) cudaEventRecord(ev[k], st);
@@ -707,7 +746,19 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   if ((e = cudaMemsetAsync(pb.len_hist, 0, (size_t)(pb.seg_len + 1) * 4, st))) return e;
   mark(0);
   const uint32_t pts_blocks = (uint32_t)((pb.n_points + 255) / 256);
-  if (pb.n_points > 0) k_count<<<pts_blocks, 256, 0, st>>>(pb);
+  if (pb.n_points > 0) {
+    if (chunk_ready && nchunks > 0) {
+      // the scalars arrive in chunks on another stream: count each chunk as soon as it lands
+      const uint64_t per = (pb.n_points + nchunks - 1) / nchunks;
+      for (int c = 0; c < nchunks; c++) {
+        const uint64_t g0 = (uint64_t)c * per, g1 = g0 + per < pb.n_points ? g0 + per : pb.n_points;
+        if ((e = cudaStreamWaitEvent(st, chunk_ready[c], 0))) return e;
+        if (g1 > g0) k_count<<<(uint32_t)((g1 - g0 + 255) / 256), 256, 0, st>>>(pb, g0, g1);
+      }
+    } else {
+      k_count<<<pts_blocks, 256, 0, st>>>(pb, 0, pb.n_points);
+    }
+  }
   mark(1);
   const uint32_t nblk = (pb.n_buckets + kScanBlock - 1) / kScanBlock;
   if (nblk > 0) {
