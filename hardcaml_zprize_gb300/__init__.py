@@ -36,7 +36,8 @@ EXPORTED = [
     "msm_last_pass_stats", "msm_server_create", "msm_server_submit", "msm_server_poll",
     "msm_server_stats", "msm_server_destroy", "msm_generate_bases", "msm_generate_scalars",
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
-    "msm_mult_noalloc", "msm_measure_int_peaks",
+    "msm_mult_noalloc", "msm_measure_int_peaks", "msm_fq_to_montgomery", "msm_fq_from_montgomery",
+    "msm_fr_to_montgomery", "msm_fr_from_montgomery",
 ]
 
 STAGES = ["count", "scan", "scatter", "tasks", "accumulate", "merge", "reduce1", "reduce2",
@@ -98,6 +99,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "msm_measure_madd_rate": (ctypes.c_double, [P, I32]),
         "msm_mult_noalloc": (ctypes.c_int, [P, P, U64, U64, P, P]),
         "msm_measure_int_peaks": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), I32]),
+        "msm_fq_to_montgomery": (ctypes.c_int, [P, U64]),
+        "msm_fq_from_montgomery": (ctypes.c_int, [P, U64]),
+        "msm_fr_to_montgomery": (ctypes.c_int, [P, U64]),
+        "msm_fr_from_montgomery": (ctypes.c_int, [P, U64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

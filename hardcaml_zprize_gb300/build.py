@@ -19,7 +19,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libdriver.so")
-SOURCES = ["msm_pipeline.cu", "msm_aux.cu", "msm_driver.cu"]
+SOURCES = ["msm_pipeline.cu", "msm_aux.cu", "msm_driver.cu", "msm_formats.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,7 +44,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         path = os.path.join(CSRC, src)
         if not force and _newer(obj, [path] + headers):
             return obj, ""

@@ -647,6 +647,27 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
 // ---------------------------------------------------------------------------------------------
 // init: resident bases
 // ---------------------------------------------------------------------------------------------
+// Tuned configurations persisted by msm_tune (one line per size class:
+// "log2n c signed seg_len red_log2 ms"); the last line for a size class wins.
+void load_tune_cache(Ctx *cx) {
+  const char *path = getenv("MSM_TUNE_CACHE");
+  if (!path) return;
+  FILE *f = fopen(path, "r");
+  if (!f) return;
+  unsigned lg, c, sg, seg, red;
+  double ms;
+  while (fscanf(f, "%u %u %u %u %u %lf", &lg, &c, &sg, &seg, &red, &ms) == 6) {
+    if (lg > 40 || c < 4 || c > 22 || seg == 0 || seg > 4096 || red > 12) continue;
+    Cfg cf;
+    cf.c = c;
+    cf.signed_digits = sg ? 1 : 0;
+    cf.seg_len = seg;
+    cf.red_log2 = red;
+    cx->tuned[lg] = cf;
+  }
+  fclose(f);
+}
+
 int init_device(Ctx *cx) {
   const char *dev = getenv("MSM_DEVICE");
   cx->device = dev ? atoi(dev) : 0;
@@ -1036,6 +1057,7 @@ void *msm_init(const char *xclbin, ssize_t xclbin_len, const g1_affine_t *points
     return nullptr;
   }
   auto *cx = new Ctx();
+  load_tune_cache(cx);
   if (init_device(cx) || load_bases(cx, points, (uint64_t)npoints)) {
     fprintf(stderr, "msm_init: %s\n", g_msg);
     delete cx;

@@ -155,6 +155,18 @@ int msm_server_poll(void *server, int64_t id, g1_projective_t *out, int32_t wait
 int msm_server_stats(void *server, msm_server_stats_t *stats);
 void msm_server_destroy(void *server);
 
+/* ---- data formats either side of the path ----
+ * The harness's test-data files (TEST_LOAD_DATA_FROM / TEST_WRITE_DATA_TO,
+ * test_fpga_harness/src/util.rs:126-172) hold ark-serialize canonical field elements; the ABI
+ * above carries arkworks' Montgomery form.  In place on n elements, all host cores:
+ *   Fq (6 x u64): x <-> x * 2^384 mod q;  Fr (4 x u64): v <-> v * 2^256 mod r (the raw integer
+ *   the harness transmutes out of Fr, tests/msm.rs:30-32).
+ * Return 0, or -3 when an input is not below the modulus. */
+int msm_fq_to_montgomery(uint64_t *v, uint64_t n);
+int msm_fq_from_montgomery(uint64_t *v, uint64_t n);
+int msm_fr_to_montgomery(uint64_t *v, uint64_t n);
+int msm_fr_from_montgomery(uint64_t *v, uint64_t n);
+
 /* ---- utilities for tests and benchmarks ---- */
 /* Bases k_i * G, k_i a seeded counter-based 64-bit draw (SplitMix64), computed on the GPU. */
 int msm_generate_bases(uint64_t seed, uint64_t first, uint64_t n, g1_affine_t *out);

@@ -281,16 +281,25 @@ def test_server_results_alone_and_in_the_mix(engine, ocpu):
         ctx.close()
 
 
-def test_tuner_keeps_results_exact(engine, ocpu):
+def test_tuner_keeps_results_exact(engine, ocpu, tmp_path, monkeypatch):
     n = 1 << 12
     pts = ocpu.gen_bases(55, n)
     sc = engine.generate_scalars(56, n)
+    cache = str(tmp_path / "tune.txt")
+    monkeypatch.setenv("MSM_TUNE_CACHE", cache)
     ctx = engine.multi_scalar_mult_init(pts)
     try:
         best = ctx.tune(n, budget_ms=5000)
         assert 6 <= best["window_bits"] <= 21
         assert ctx.config(n)["window_bits"] == best["window_bits"]
         assert np.array_equal(ctx.mult(sc)[0], ocpu.msm(pts, sc))
+    finally:
+        ctx.close()
+    # a new context picks the tuned configuration up from the cache file
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        assert ctx.config(n)["window_bits"] == best["window_bits"]
+        assert ctx.config(n)["seg_len"] == best["seg_len"]
     finally:
         ctx.close()
 
@@ -362,3 +371,23 @@ def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
         assert ref.decode_projective(out[0].tobytes()) == ref.msm_naive(pts_l, ks2)
     finally:
         ctx.close()
+
+
+def test_msm_correctness_from_test_data_files(engine, ref, ocpu, tmp_path):
+    """msm_correctness with TEST_LOAD_DATA_FROM (tests/msm.rs:15-42, util.rs:236-257): the data
+    directory is written in the harness's format, loaded back, run, and checked batch by batch."""
+    from hardcaml_zprize_gb300 import arkworks_io as io
+    n, batches = 1 << 10, 4
+    pts = ocpu.gen_bases(11, n)
+    sc = engine.generate_scalars(12, n * batches)
+    expected = np.stack([ocpu.msm(pts, sc[b * n:(b + 1) * n]) for b in range(batches)])
+    d = str(tmp_path / "testdata")
+    io.save_test_data(d, pts, sc, expected)
+    nb, points, scalars, results = io.load_test_data(d)
+    ctx = engine.multi_scalar_mult_init(points)
+    try:
+        out = engine.multi_scalar_mult(ctx, points, scalars)
+    finally:
+        ctx.close()
+    assert nb == batches
+    assert np.array_equal(io.projective_to_affine_records(out), results)
