@@ -279,7 +279,7 @@ def run_ours(args, rank, world, local):
                    "fixed_base_tables": cfg["fixed_base"] == 1},
         "e2e": {"value": e2e, "unit": "MSM/s", "h2d_bytes_per_step": n * 32,
                 "d2h_bytes_per_step": 144},
-        "gpu_launches": 11 * args.steps,
+        "gpu_launches": int(stats["kernels"]) * args.steps,  # counted by the driver per pass
         "points_per_s": value * n,
         "latency_ms": {"p50": 1e3 * percentile(lat, 50), "p99": 1e3 * percentile(lat, 99)},
         "roofline": {

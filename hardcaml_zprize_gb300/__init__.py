@@ -224,9 +224,10 @@ class MultiScalarMultContext:
         return {STAGES[k]: arr[k] for k in range(n)}
 
     def last_pass_stats(self) -> dict:
-        arr = (ctypes.c_uint64 * 4)()
-        load_library().msm_last_pass_stats(self.handle, arr, 4)
-        return {"tasks": arr[0], "heavy_buckets": arr[1], "max_entries": arr[2], "buckets": arr[3]}
+        arr = (ctypes.c_uint64 * 5)()
+        load_library().msm_last_pass_stats(self.handle, arr, 5)
+        return {"tasks": arr[0], "heavy_buckets": arr[1], "max_entries": arr[2], "buckets": arr[3],
+                "kernels": arr[4]}
 
     def mult_noalloc(self, n: int, base_offset: int, d_scalars_ptr: int, d_out_ptr: int,
                      stream: int = 0) -> None:

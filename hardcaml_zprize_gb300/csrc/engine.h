@@ -114,11 +114,13 @@ struct PassBuffers {
 // `stage_events` (10 events, or null) are recorded around the stages for per-kernel timing
 // `chunk_ready` (nchunks events, or null): the scalars arrive in nchunks equal point ranges and
 // the histogram of range c waits for event c (copy/compute overlap for host-resident scalars)
+// `n_kernels` (or null) receives the number of kernels launched
 cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t stream,
                             cudaEvent_t *stage_events, const cudaEvent_t *chunk_ready = nullptr,
-                            int nchunks = 0);
+                            int nchunks = 0, uint32_t *n_kernels = nullptr);
 #define MSM_NUM_STAGES 10
 size_t msm_scan_tmp_words(uint32_t n_buckets);
+uint32_t msm_scatter_passes(uint64_t max_entries);
 
 // resident-base preparation
 cudaError_t msm_launch_precompute(const void *d_affine, size_t n, uint4 *d_bases, uint8_t *d_flags,

@@ -309,10 +309,14 @@ struct Workspace {
   HostPinned res_host;
   cudaEvent_t ev[MSM_NUM_STAGES + 1] = {};
   uint64_t generation = 0;  // bumps when any buffer moves (graphs must be re-captured)
-  std::unordered_map<std::string, cudaGraphExec_t> graphs;
+  struct GraphEntry {
+    cudaGraphExec_t exec;
+    uint32_t kernels;  // kernel launches in one replay
+  };
+  std::unordered_map<std::string, GraphEntry> graphs;
 
   ~Workspace() {
-    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
   }
@@ -341,13 +345,13 @@ struct Workspace {
       for (auto &e : ev) CK(cudaEventCreate(&e));
     if (moved) {
       generation++;
-      for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+      for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
       graphs.clear();
     }
     return 0;
   }
   [[maybe_unused]] void release_sort_buffers() {
-    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
     graphs.clear();
     count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
     scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
@@ -375,7 +379,7 @@ struct Ctx {
   std::mutex mu;
   bool timing = false;
   double last_ms[MSM_NUM_STAGES] = {0};
-  uint64_t last_stats[4] = {0};
+  uint64_t last_stats[5] = {0};  // tasks, heavy buckets, sorted entries, buckets, kernels
   std::map<uint32_t, Cfg> tuned;  // by log2 size class
   ~Ctx() {
     if (stream) cudaStreamDestroy(stream);
@@ -455,8 +459,9 @@ int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, 
     auto it = ws.graphs.find(key);
     if (it == ws.graphs.end()) {
       cudaGraph_t g;
+      uint32_t nk = 0;
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e = msm_launch_pass(pb, cx->num_sms, st, nullptr);
+      cudaError_t e = msm_launch_pass(pb, cx->num_sms, st, nullptr, nullptr, 0, &nk);
       cudaError_t e2 = cudaMemcpyAsync(res_dst, ws.results.p, pl.jobs.size() * MSM_PROJ_BYTES,
                                        cudaMemcpyDeviceToHost, st);
       cudaError_t e3 = cudaStreamEndCapture(st, &g);
@@ -466,12 +471,15 @@ int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, 
       cudaGraphExec_t ex;
       CK(cudaGraphInstantiate(&ex, g, 0));
       cudaGraphDestroy(g);
-      it = ws.graphs.emplace(key, ex).first;
+      it = ws.graphs.emplace(key, Workspace::GraphEntry{ex, nk}).first;
     }
-    CK(cudaGraphLaunch(it->second, st));
+    CK(cudaGraphLaunch(it->second.exec, st));
+    cx->last_stats[4] = it->second.kernels;
     return 0;
   }
-  CK(msm_launch_pass(pb, cx->num_sms, st, timing ? ws.ev : nullptr, chunk_ready, nchunks));
+  uint32_t nk = 0;
+  CK(msm_launch_pass(pb, cx->num_sms, st, timing ? ws.ev : nullptr, chunk_ready, nchunks, &nk));
+  cx->last_stats[4] = nk;
   CK(cudaMemcpyAsync(res_dst, ws.results.p, pl.jobs.size() * MSM_PROJ_BYTES,
                      cudaMemcpyDeviceToHost, st));
   return 0;
@@ -1151,7 +1159,7 @@ int msm_last_timings(void *context, double *ms, int32_t max_stages) {
 int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats) {
   auto *cx = (Ctx *)context;
   if (!cx || !stats) return fail(ERR_ARG, "null argument");
-  const int n = std::min<int>(max_stats, 4);
+  const int n = std::min<int>(max_stats, 5);
   for (int k = 0; k < n; k++) stats[k] = cx->last_stats[k];
   return n;
 }

@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(PassBuffers pb) {
   for (int k = 0; k < kScanItems; k++) {
     if (base + k < pb.n_buckets) {
       pb.offset[base + k] = ex.x;
+      pb.fill[base + k] = ex.x;  // the scatter's slot cursor starts at the bucket's offset
       pb.taskoff[base + k] = ex.y;
     }
     ex.x += c[k];
@@ -220,9 +221,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(PassBuffers pb) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// 3. scatter into bucket order
+// 3. scatter into bucket order, one launch per range of bucket keys [key_lo, key_hi).  A range's
+//    slice of the sorted array is a few hundred MB, so its random 4-byte stores mostly merge in
+//    L2 instead of each costing a DRAM read-modify-write of a whole sector; every launch
+//    recomputes the digits and keeps only the entries in its range.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_scatter(PassBuffers pb) {
+__global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
   const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= pb.n_points) return;
   if (pb.counters[CNT_ERROR]) return;
@@ -234,11 +238,12 @@ __global__ void k_scatter(PassBuffers pb) {
   const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
   const int lane = threadIdx.x & 31;
   uint32_t carry = 0;
-  // four windows per step: their slot atomics and offset loads are independent, so the four
-  // round trips overlap instead of running one after another
+  // four windows per step: their slot atomics are independent, so the four round trips
+  // overlap instead of running one after another.  fill[key] starts at the bucket's offset in
+  // the sorted array, so the atomic returns the entry's position directly.
 #pragma unroll 1
   for (uint32_t w0 = 0; w0 < jd.nwin; w0 += 4) {
-    uint32_t key[4], val[4], slot[4], base[4];
+    uint32_t key[4], val[4], pos[4];
     bool ok[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -251,6 +256,7 @@ __global__ void k_scatter(PassBuffers pb) {
         if (d != 0) {
           ok[k] = true;
           key[k] = bucket_key(jd, w, (uint32_t)abs(d));
+          ok[k] = key[k] >= key_lo && key[k] < key_hi;
           const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
           val[k] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
         }
@@ -258,8 +264,7 @@ __global__ void k_scatter(PassBuffers pb) {
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      slot[k] = 0;
-      base[k] = 0;
+      pos[k] = 0;
       if (ok[k]) {
         const uint32_t active = __activemask();
         const int leader = __ffs(active) - 1;
@@ -267,21 +272,19 @@ __global__ void k_scatter(PassBuffers pb) {
         if (__all_sync(active, key[k] == k0)) {  // one bucket for the whole warp: one atomic
           uint32_t bp = 0;
           if (lane == leader) bp = atomicAdd(&pb.fill[key[k]], (uint32_t)__popc(active));
-          slot[k] = __shfl_sync(active, bp, leader) + __popc(active & ((1u << lane) - 1u));
+          pos[k] = __shfl_sync(active, bp, leader) + __popc(active & ((1u << lane) - 1u));
         } else {
-          slot[k] = atomicAdd(&pb.fill[key[k]], 1u);
+          pos[k] = atomicAdd(&pb.fill[key[k]], 1u);
         }
-        base[k] = pb.offset[key[k]];
       }
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (!ok[k]) continue;
-      const uint64_t pos = (uint64_t)base[k] + slot[k];
-      if (pos < pb.max_entries) {
-        pb.vals[pos] = val[k];
+      if (pos[k] < pb.max_entries) {
+        pb.vals[pos[k]] = val[k];
       } else {
-        set_error(pb.counters, 3, (uint32_t)pos);
+        set_error(pb.counters, 3, pos[k]);
       }
     }
   }
@@ -730,18 +733,26 @@ __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
 
 }  // namespace
 
+// Scatter launches per pass: one per ~200 MB of sorted array, at most 8 (on GB300 the best
+// counts measured were 4 for 2^24 points x 12 windows and 8 for 2^26 x 11 windows).
+uint32_t msm_scatter_passes(uint64_t max_entries) {
+  const uint64_t bytes = max_entries * 4, per = 200ull << 20;
+  const uint64_t p = (bytes + per / 2) / per;
+  return (uint32_t)(p < 1 ? 1 : p > 8 ? 8 : p);
+}
+
 size_t msm_scan_tmp_words(uint32_t n_buckets) {
   return 2ull * ((n_buckets + kScanBlock - 1) / kScanBlock) + 2;
 }
 
 cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st, cudaEvent_t *ev,
-                            const cudaEvent_t *chunk_ready, int nchunks) {
+                            const cudaEvent_t *chunk_ready, int nchunks, uint32_t *n_kernels) {
   cudaError_t e;
+  uint32_t launched = 0;
   auto mark = [&](int k) {
     if (ev) cudaEventRecord(ev[k], st);
   };
   if ((e = cudaMemsetAsync(pb.count, 0, (size_t)pb.n_buckets * 4, st))) return e;
-  if ((e = cudaMemsetAsync(pb.fill, 0, (size_t)pb.n_buckets * 4, st))) return e;
   if ((e = cudaMemsetAsync(pb.counters, 0, CNT_WORDS * 4, st))) return e;
   if ((e = cudaMemsetAsync(pb.len_hist, 0, (size_t)(pb.seg_len + 1) * 4, st))) return e;
   mark(0);
@@ -753,39 +764,72 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
       for (int c = 0; c < nchunks; c++) {
         const uint64_t g0 = (uint64_t)c * per, g1 = g0 + per < pb.n_points ? g0 + per : pb.n_points;
         if ((e = cudaStreamWaitEvent(st, chunk_ready[c], 0))) return e;
-        if (g1 > g0) k_count<<<(uint32_t)((g1 - g0 + 255) / 256), 256, 0, st>>>(pb, g0, g1);
+        if (g1 > g0) {
+          k_count<<<(uint32_t)((g1 - g0 + 255) / 256), 256, 0, st>>>(pb, g0, g1);
+          launched++;
+        }
       }
     } else {
       k_count<<<pts_blocks, 256, 0, st>>>(pb, 0, pb.n_points);
+      launched++;
     }
   }
   mark(1);
   const uint32_t nblk = (pb.n_buckets + kScanBlock - 1) / kScanBlock;
   if (nblk > 0) {
     k_scan_reduce<<<nblk, kScanThreads, 0, st>>>(pb);
+    launched++;
     k_scan_blocks<<<1, kScanThreads, 0, st>>>(pb, nblk);
+    launched++;
     k_scan_apply<<<nblk, kScanThreads, 0, st>>>(pb);
+    launched++;
   }
   mark(2);
-  if (pb.n_points > 0) k_scatter<<<pts_blocks, 256, 0, st>>>(pb);
+  if (pb.n_points > 0) {
+    const uint32_t passes = msm_scatter_passes(pb.max_entries);
+    for (uint32_t p = 0; p < passes; p++) {
+      const uint32_t lo = (uint32_t)((uint64_t)pb.n_buckets * p / passes);
+      const uint32_t hi = (uint32_t)((uint64_t)pb.n_buckets * (p + 1) / passes);
+      k_scatter<<<pts_blocks, 256, 0, st>>>(pb, lo, hi);
+      launched++;
+    }
+  }
   mark(3);
   if (pb.n_buckets > 0) {
     k_len_hist<<<num_sms * 4, 256, (pb.seg_len + 1) * 4, st>>>(pb);
+    launched++;
     k_len_scan<<<1, 32, 0, st>>>(pb);
+    launched++;
     k_tasks<<<(pb.n_buckets + 255) / 256, 256, 0, st>>>(pb);
+    launched++;
   }
   mark(4);
   k_accumulate<<<num_sms * 4, 128, 0, st>>>(pb);
+  launched++;
   mark(5);
   k_merge<<<num_sms, 256, 0, st>>>(pb);
+  launched++;
   mark(6);
-  if (pb.n_segs > 0) k_reduce1<<<(pb.n_segs + 127) / 128, 128, 0, st>>>(pb);
+  if (pb.n_segs > 0) {
+    k_reduce1<<<(pb.n_segs + 127) / 128, 128, 0, st>>>(pb);
+    launched++;
+  }
   mark(7);
-  if (pb.n_grps > 0) k_reduce2<<<pb.n_grps, kRedThreads, 0, st>>>(pb);
+  if (pb.n_grps > 0) {
+    k_reduce2<<<pb.n_grps, kRedThreads, 0, st>>>(pb);
+    launched++;
+  }
   mark(8);
-  if (pb.n_wins > 0) k_reduce3<<<pb.n_wins, kRedThreads, 0, st>>>(pb);
+  if (pb.n_wins > 0) {
+    k_reduce3<<<pb.n_wins, kRedThreads, 0, st>>>(pb);
+    launched++;
+  }
   mark(9);
-  if (pb.n_jobs > 0) k_final<<<pb.n_jobs, 128, 0, st>>>(pb);
+  if (pb.n_jobs > 0) {
+    k_final<<<pb.n_jobs, 128, 0, st>>>(pb);
+    launched++;
+  }
   mark(10);
+  if (n_kernels) *n_kernels = launched;
   return cudaGetLastError();
 }

@@ -118,7 +118,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
  * merge, reduce1, reduce2, reduce3, final. Returns the number of stages written. */
 int msm_set_timing(void *context, int32_t enable);
 int msm_last_timings(void *context, double *ms, int32_t max_stages);
-/* Counters of the last pass: tasks, heavy buckets, sorted entries, buckets. */
+/* Counters of the last pass: tasks, heavy buckets, sorted entries, buckets, kernel launches. */
 int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats);
 
 /* One MSM that allocates no device memory; it has no counterpart in the reference.
