@@ -78,6 +78,8 @@ struct PassBuffers {
   uint64_t n_bases;             // resident bases (bounds of every base index)
 
   const uint4 *scalars;         // 2 x uint4 per scalar
+  const uint4 *host_scalars;    // or null: k_count first copies each scalar from this host buffer
+                                // (same indexing) into `scalars`, reading over the C2C link
   const JobDesc *jobs;
   const WinDesc *wins;
   uint32_t n_jobs;

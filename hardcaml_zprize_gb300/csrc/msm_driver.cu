@@ -375,6 +375,9 @@ struct Ctx {
   cudaEvent_t copied[2] = {}, freed[2] = {};
   static constexpr int kCopyChunks = 4;
   cudaEvent_t chunk_ev[2][kCopyChunks] = {};
+  // the device reads pageable host memory coherently (Grace: ATS over NVLink-C2C), so host
+  // scalars are uploaded by the histogram kernel itself instead of a separate copy
+  bool host_pull = false;
   Workspace ws;
   std::mutex mu;
   bool timing = false;
@@ -440,19 +443,21 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
 // graph), copy the results to ws.res_host + res_offset jobs.  Does not synchronize.
 int enqueue_pass(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars, cudaStream_t st,
                  bool use_graph, bool timing, size_t res_offset,
-                 const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0) {
+                 const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0,
+                 const void *host_src = nullptr) {
   if (ws.ensure(pl)) return g_err;
   CK(cudaMemcpyAsync(ws.jobs.p, pl.jobs.data(), pl.jobs.size() * sizeof(JobDesc),
                      cudaMemcpyHostToDevice, st));
   if (!pl.wins.empty())
     CK(cudaMemcpyAsync(ws.wins.p, pl.wins.data(), pl.wins.size() * sizeof(WinDesc),
                        cudaMemcpyHostToDevice, st));
-  const PassBuffers pb = make_pass_buffers(cx, ws, pl, d_scalars);
+  PassBuffers pb = make_pass_buffers(cx, ws, pl, d_scalars);
+  pb.host_scalars = (const uint4 *)host_src;
   char *res_dst = (char *)ws.res_host.p;
   if (res_offset * MSM_PROJ_BYTES + pl.jobs.size() * MSM_PROJ_BYTES > ws.res_host.bytes)
     return fail(ERR_STATE, "result staging too small");
   res_dst += res_offset * MSM_PROJ_BYTES;
-  if (use_graph && !timing && !chunk_ready) {
+  if (use_graph && !timing && !chunk_ready && !host_src) {
     char tmp[64];
     snprintf(tmp, sizeof(tmp), "#%p#%p", d_scalars, (void *)res_dst);
     const std::string key = pl.key + tmp;
@@ -547,6 +552,12 @@ void record_timings(Ctx *cx, Workspace &ws) {
   }
 }
 
+// Host scalars the histogram kernel may read directly: the device reads pageable memory and the
+// buffer is 16-byte aligned (the kernel loads uint4).
+bool host_pullable(const Ctx *cx, const void *h) {
+  return cx->host_pull && h && ((uintptr_t)h & 15u) == 0;
+}
+
 // Run a list of MSMs whose scalars are in host memory (d_scalars == nullptr) or already on the
 // device.  mode 1: one pass per MSM with the next MSM's scalars copied during the current pass;
 // mode 2: all MSMs in one pass with one shared sort.
@@ -578,14 +589,19 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     }
     Plan pl;
     if (build_plan(specs, pl)) return g_err;
-    const void *src = d_scalars;
+    const void *src = d_scalars, *pull = nullptr;
     if (!src) {
       CK(ws.scalars[0].ensure(first[m] * 32));
-      if (first[m]) CK(cudaMemcpyAsync(ws.scalars[0].p, h_scalars, first[m] * 32,
-                                       cudaMemcpyHostToDevice, cx->stream));
+      if (host_pullable(cx, h_scalars)) {
+        pull = h_scalars;
+      } else if (first[m]) {
+        CK(cudaMemcpyAsync(ws.scalars[0].p, h_scalars, first[m] * 32, cudaMemcpyHostToDevice,
+                           cx->stream));
+      }
       src = ws.scalars[0].p;
     }
-    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, 0)) return g_err;
+    if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, 0, nullptr, 0, pull))
+      return g_err;
     if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
     if (cx->timing) record_timings(cx, ws);
     cx->last_stats[2] = pl.max_entries;
@@ -616,9 +632,13 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
     Plan pl;
     if (build_plan(one, pl)) return g_err;
-    const void *src = d_scalars;
+    const void *src = d_scalars, *pull = nullptr;
     const cudaEvent_t *chunks = nullptr;
-    if (!src) {
+    if (!src && host_pullable(cx, h_scalars + first[j])) {
+      // the histogram kernel reads the scalars from host memory and leaves the device copy
+      src = ws.scalars[(int)(j & 1)].p;
+      pull = h_scalars + first[j];
+    } else if (!src) {
       // the copy goes up in chunks on the copy stream; each chunk's histogram starts when it lands
       const int slot = (int)(j & 1);
       const int nch = Ctx::kCopyChunks;
@@ -637,7 +657,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
       chunks = cx->chunk_ev[slot];
     }
     if (enqueue_pass(cx, ws, pl, src, cx->stream, use_graph, cx->timing, j, chunks,
-                     chunks ? Ctx::kCopyChunks : 0))
+                     chunks ? Ctx::kCopyChunks : 0, pull))
       return g_err;
     if (!d_scalars) CK(cudaEventRecord(cx->freed[(int)(j & 1)], cx->stream));
     if (cx->timing) {
@@ -683,6 +703,10 @@ int init_device(Ctx *cx) {
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, cx->device));
   cx->num_sms = prop.multiProcessorCount;
+  int pageable = 0;
+  CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, cx->device));
+  const char *hp = getenv("MSM_HOST_PULL");
+  cx->host_pull = pageable != 0 && !(hp && strcmp(hp, "0") == 0);
   CK(cudaStreamCreateWithFlags(&cx->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&cx->copy_stream, cudaStreamNonBlocking));
   for (int i = 0; i < 2; i++) {

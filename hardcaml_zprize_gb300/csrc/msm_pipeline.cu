@@ -41,14 +41,15 @@ struct ScalarBits {
   uint32_t w[9];
 };
 
-__device__ __forceinline__ ScalarBits load_scalar(const uint4 *p) {
-  const uint4 a = p[0], b = p[1];
+__device__ __forceinline__ ScalarBits scalar_bits(const uint4 &a, const uint4 &b) {
   ScalarBits s;
   s.w[0] = a.x; s.w[1] = a.y; s.w[2] = a.z; s.w[3] = a.w;
   s.w[4] = b.x; s.w[5] = b.y; s.w[6] = b.z; s.w[7] = b.w & 0x1fffffffu;
   s.w[8] = 0;
   return s;
 }
+
+__device__ __forceinline__ ScalarBits load_scalar(const uint4 *p) { return scalar_bits(p[0], p[1]); }
 
 __device__ __forceinline__ uint32_t slice_bits(const ScalarBits &s, uint32_t off, uint32_t c) {
   const uint32_t k = off >> 5;
@@ -83,14 +84,8 @@ __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, ui
 // ---------------------------------------------------------------------------------------------
 // 1. histogram
 // ---------------------------------------------------------------------------------------------
-__global__ void k_count(PassBuffers pb, uint64_t g_begin, uint64_t g_end) {
-  const uint64_t g = g_begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= g_end || g >= pb.n_points) return;
-  const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
-  const JobDesc jd = pb.jobs[j];
-  const uint64_t i = g - jd.point_begin;
-  if (pb.flags[jd.base_off + i] != BASE_OK) return;
-  const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
+__device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd,
+                                             const ScalarBits &s) {
   uint32_t carry = 0;
   for (uint32_t w = 0; w < jd.nwin; w++) {
     const int32_t d = window_digit(s, jd, w, carry);
@@ -106,6 +101,28 @@ __global__ void k_count(PassBuffers pb, uint64_t g_begin, uint64_t g_end) {
     } else {
       atomicAdd(&pb.count[key], 1u);
     }
+  }
+}
+
+__global__ void k_count(PassBuffers pb, uint64_t g_begin, uint64_t g_end) {
+  const uint64_t g = g_begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= g_end || g >= pb.n_points) return;
+  const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
+  const JobDesc jd = pb.jobs[j];
+  const uint64_t i = g - jd.point_begin;
+  const uint64_t si = 2 * (jd.scalar_off + i);
+  if (pb.host_scalars) {
+    // fused upload: every scalar of the pass (bases without a bucket entry included, k_final
+    // reads theirs) goes from host memory to the device copy the later kernels read
+    const uint4 a = pb.host_scalars[si], b = pb.host_scalars[si + 1];
+    uint4 *dst = const_cast<uint4 *>(pb.scalars) + si;
+    dst[0] = a;
+    dst[1] = b;
+    if (pb.flags[jd.base_off + i] != BASE_OK) return;
+    count_digits(pb, jd, scalar_bits(a, b));
+  } else {
+    if (pb.flags[jd.base_off + i] != BASE_OK) return;
+    count_digits(pb, jd, load_scalar(pb.scalars + si));
   }
 }
 

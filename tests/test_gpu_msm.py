@@ -248,6 +248,37 @@ def test_uneven_batch_modes(engine, ocpu):
         ctx.close()
 
 
+def test_host_scalar_upload_paths(engine, ocpu, monkeypatch):
+    """Host scalars reach the device through the histogram kernel's own reads of host memory (a
+    device that reads pageable memory, 16-byte aligned buffer) or through chunked copies
+    (MSM_HOST_PULL=0, or a buffer at an address that is 8 mod 16); every path, in both pass modes,
+    gives the oracle's results."""
+    nb = 1 << 12
+    pts = ocpu.gen_bases(31, nb)
+    sizes = [4096, 7, 1000, 0, 2500]
+    offs = [0, 4000, 17, 5, 1596]
+    sc = np.concatenate([engine.generate_scalars(40 + j, s) for j, s in enumerate(sizes)])
+    raw = np.empty(sc.size + 2, dtype=np.uint64)
+    start = 1 if raw.ctypes.data % 16 == 0 else 0
+    mis = raw[start:start + sc.size]
+    mis[:] = sc.reshape(-1)
+    assert mis.ctypes.data % 16 == 8
+    mis = mis.reshape(sc.shape)
+    first = np.concatenate([[0], np.cumsum(sizes)])
+    want = [ocpu.msm(pts[o:o + s], sc[first[j]:first[j] + s]) for j, (s, o) in enumerate(zip(sizes, offs))]
+    for pull in ("1", "0"):
+        monkeypatch.setenv("MSM_HOST_PULL", pull)
+        ctx = engine.multi_scalar_mult_init(pts)
+        try:
+            for buf in (sc, mis):
+                for mode in (1, 2):
+                    out = ctx.mult_uneven(sizes, offs, buf, mode=mode)
+                    for j in range(len(sizes)):
+                        assert np.array_equal(out[j], want[j]), (pull, buf is mis, mode, j)
+        finally:
+            ctx.close()
+
+
 def test_server_results_alone_and_in_the_mix(engine, ocpu):
     nb = 1 << 12
     pts = ocpu.gen_bases(8, nb)
