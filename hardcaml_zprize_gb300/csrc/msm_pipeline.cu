@@ -36,35 +36,38 @@ __device__ __forceinline__ uint32_t find_job(const JobDesc *jobs, uint32_t n_job
   return lo;
 }
 
-// scalar as 8 little-endian words plus a zero guard word, masked to 253 bits
+// The scalar bits not yet consumed, least significant first, masked to 253 bits on load.
+// Windows are taken in order: each take shifts the whole scalar right by c (funnel shifts in
+// registers; a runtime word index into the scalar would compile to select chains).
 struct ScalarBits {
-  uint32_t w[9];
+  uint32_t w[8];
 };
 
 __device__ __forceinline__ ScalarBits scalar_bits(const uint4 &a, const uint4 &b) {
   ScalarBits s;
   s.w[0] = a.x; s.w[1] = a.y; s.w[2] = a.z; s.w[3] = a.w;
   s.w[4] = b.x; s.w[5] = b.y; s.w[6] = b.z; s.w[7] = b.w & 0x1fffffffu;
-  s.w[8] = 0;
   return s;
 }
 
 __device__ __forceinline__ ScalarBits load_scalar(const uint4 *p) { return scalar_bits(p[0], p[1]); }
 
-__device__ __forceinline__ uint32_t slice_bits(const ScalarBits &s, uint32_t off, uint32_t c) {
-  const uint32_t k = off >> 5;
-  const uint64_t two = ((uint64_t)s.w[k < 8 ? k + 1 : 8] << 32) | s.w[k < 9 ? k : 8];
-  return (uint32_t)(two >> (off & 31)) & ((1u << c) - 1u);
+// the next c bits (1 <= c <= 31); bits past 253 read as zero
+__device__ __forceinline__ uint32_t take_bits(ScalarBits &s, uint32_t c) {
+  const uint32_t v = s.w[0] & ((1u << c) - 1u);
+#pragma unroll
+  for (int k = 0; k < 7; k++) s.w[k] = __funnelshift_r(s.w[k], s.w[k + 1], c);
+  s.w[7] >>= c;
+  return v;
 }
 
-// Digit of window w given the running carry (hardcaml/test/top/utils.ml:243-288): slice + carry;
-// below the top window a value >= 2^(c-1) becomes value - 2^c with carry 1.  Returns the signed
-// digit and updates carry.  Unsigned mode returns the plain slice.
-__device__ __forceinline__ int32_t window_digit(const ScalarBits &s, const JobDesc &jd, uint32_t w,
-                                                uint32_t &carry) {
-  const uint32_t off = w * jd.c;
-  const uint32_t width = min(jd.c, (uint32_t)MSM_SCALAR_BITS - off);
-  int32_t d = (int32_t)(slice_bits(s, off, width) + carry);
+// Digit of window w, the windows taken in order from 0, given the running carry
+// (hardcaml/test/top/utils.ml:243-288): slice + carry; below the top window a value >= 2^(c-1)
+// becomes value - 2^c with carry 1.  Returns the signed digit and updates carry.  Unsigned mode
+// returns the plain slice.
+__device__ __forceinline__ int32_t next_digit(ScalarBits &s, const JobDesc &jd, uint32_t w,
+                                              uint32_t &carry) {
+  int32_t d = (int32_t)(take_bits(s, jd.c) + carry);
   if (!jd.signed_digits) return d;
   if (w + 1 < jd.nwin && d >= (int32_t)(1u << (jd.c - 1))) {
     d -= (int32_t)(1u << jd.c);
@@ -84,11 +87,10 @@ __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, ui
 // ---------------------------------------------------------------------------------------------
 // 1. histogram
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd,
-                                             const ScalarBits &s) {
+__device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s) {
   uint32_t carry = 0;
   for (uint32_t w = 0; w < jd.nwin; w++) {
-    const int32_t d = window_digit(s, jd, w, carry);
+    const int32_t d = next_digit(s, jd, w, carry);
     if (d == 0) continue;
     const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
     // a warp whose active lanes all hit one bucket (e.g. equal scalars) adds once; otherwise
@@ -252,7 +254,7 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
   const uint64_t i = g - jd.point_begin;
   const uint64_t bidx = jd.base_off + i;
   if (pb.flags[bidx] != BASE_OK) return;
-  const ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
+  ScalarBits s = load_scalar(pb.scalars + 2 * (jd.scalar_off + i));
   const int lane = threadIdx.x & 31;
   uint32_t carry = 0;
   // four windows per step: their slot atomics are independent, so the four round trips
@@ -269,7 +271,7 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
       key[k] = 0;
       val[k] = 0;
       if (w < jd.nwin) {
-        const int32_t d = window_digit(s, jd, w, carry);
+        const int32_t d = next_digit(s, jd, w, carry);
         if (d != 0) {
           ok[k] = true;
           key[k] = bucket_key(jd, w, (uint32_t)abs(d));
@@ -513,84 +515,148 @@ __global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
   xyzt_store(pb.seg_out + (size_t)s * 24 + 12, A);
 }
 
-constexpr int kRedThreads = 128;
+// ---- 4-lane cooperative point operations ----
+// The four lanes of a quad (lanes 4k..4k+3 of a warp) hold the same point.  Each lane computes one
+// of four independent products and the lanes swap results, so a doubling costs two product
+// latencies instead of eight and an addition three instead of nine.  `mask` names the lanes
+// executing the call (whole quads).
+__device__ __forceinline__ fq_t shfl4(const fq_t &a, int src, uint32_t mask) {
+  fq_t r;
+#pragma unroll
+  for (int k = 0; k < FQ_LIMBS; k++) r.v[k] = __shfl_sync(mask, a.v[k], src, 4);
+  return r;
+}
+__device__ __forceinline__ fq_t pick4(int l, const fq_t &a, const fq_t &b, const fq_t &c, const fq_t &d) {
+  return fq_select(l == 0, a, fq_select(l == 1, b, fq_select(l == 2, c, d)));
+}
 
-// Sum of a block's points in shared memory; the result is valid in thread 0.
+__device__ __noinline__ xyzt_t te_dbl_quad(const xyzt_t &p, uint32_t mask) {
+  const int l = threadIdx.x & 3;
+  const fq_t sq = fq_sqr(pick4(l, p.x, p.y, p.z, fq_add(p.x, p.y)));
+  const fq_t A = shfl4(sq, 0, mask), B = shfl4(sq, 1, mask), ZZ = shfl4(sq, 2, mask), S = shfl4(sq, 3, mask);
+  const fq_t C = fq_dbl(ZZ);
+  const fq_t D = fq_neg(A);
+  const fq_t E = fq_sub(fq_sub(S, A), B);
+  const fq_t G = fq_add(D, B);
+  const fq_t F = fq_sub(G, C);
+  const fq_t H = fq_sub(D, B);
+  const fq_t pr = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
+  xyzt_t r;
+  r.x = shfl4(pr, 0, mask);
+  r.y = shfl4(pr, 1, mask);
+  r.t = shfl4(pr, 2, mask);
+  r.z = shfl4(pr, 3, mask);
+  return r;
+}
+
+__device__ __noinline__ xyzt_t te_add_quad(const xyzt_t &p, const xyzt_t &q, uint32_t mask) {
+  const uint32_t kc[FQ_LIMBS] = BLS_TE_K;
+  const int l = threadIdx.x & 3;
+  const fq_t m1 = pick4(l, fq_sub(p.y, p.x), fq_add(p.y, p.x), p.t, p.z);
+  const fq_t m2 = pick4(l, fq_sub(q.y, q.x), fq_add(q.y, q.x), q.t, q.z);
+  const fq_t pr = fq_mul(m1, m2);
+  const fq_t A = shfl4(pr, 0, mask), B = shfl4(pr, 1, mask), TT = shfl4(pr, 2, mask), ZZ = shfl4(pr, 3, mask);
+  const fq_t C = fq_mul(TT, fq_from(kc));
+  const fq_t D = fq_dbl(ZZ);
+  const fq_t E = fq_sub(B, A);
+  const fq_t F = fq_sub(D, C);
+  const fq_t G = fq_add(D, C);
+  const fq_t H = fq_add(B, A);
+  const fq_t pr2 = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
+  xyzt_t r;
+  r.x = shfl4(pr2, 0, mask);
+  r.y = shfl4(pr2, 1, mask);
+  r.t = shfl4(pr2, 2, mask);
+  r.z = shfl4(pr2, 3, mask);
+  return r;
+}
+
+constexpr int kRedThreads = 256;
+constexpr uint32_t kRedQuads = kRedThreads / 4;
+constexpr uint32_t kAllLanes = 0xffffffffu;
+
+// Levels 2 and 3 are chains of dependent additions, so they run on quads: every quad of the
+// block executes every addition (a quad with nothing to add adds the identity), which keeps the
+// warps converged for the quad shuffles.
+
+// Sum over the block's quads in shared memory; the result is valid in quad 0.  At each level
+// only the warps holding a quad below the stride add (whole warps, so their shuffles stay
+// converged).
 __device__ __forceinline__ xyzt_t block_sum(xyzt_t X, uint4 *sh) {
-  const uint32_t tid = threadIdx.x;
-  xyzt_store(sh + tid * 12, X);
+  const uint32_t q = threadIdx.x >> 2, ql = threadIdx.x & 3;
+  const uint32_t warp_q0 = (threadIdx.x >> 5) * 8;  // first quad of this warp
+  if (ql == 0) xyzt_store(sh + q * 12, X);
   __syncthreads();
 #pragma unroll 1
-  for (uint32_t stride = kRedThreads / 2; stride > 0; stride >>= 1) {
-    if (tid < stride) {
-      xyzt_t o;
-      xyzt_load(o, sh + (tid + stride) * 12);
-      X = te_add_ool(X, o);
-      xyzt_store(sh + tid * 12, X);
-    }
+  for (uint32_t stride = kRedQuads / 2; stride > 0; stride >>= 1) {
+    xyzt_t o = xyzt_identity();
+    if (q < stride) xyzt_load(o, sh + (q + stride) * 12);
+    if (warp_q0 < stride) X = te_add_quad(X, o, kAllLanes);
+    __syncthreads();
+    if (q < stride && ql == 0) xyzt_store(sh + q * 12, X);
     __syncthreads();
   }
   return X;
 }
 
-// Inclusive suffix sums over the block: thread t gets sum_{u >= t} X_u (Hillis-Steele).
+// Inclusive suffix sums over the quads: quad u gets sum_{v >= u} X_v (Hillis-Steele).
 __device__ __forceinline__ xyzt_t block_suffix_scan(xyzt_t X, uint4 *sh) {
-  const uint32_t tid = threadIdx.x;
-  xyzt_store(sh + tid * 12, X);
+  const uint32_t q = threadIdx.x >> 2, ql = threadIdx.x & 3;
+  if (ql == 0) xyzt_store(sh + q * 12, X);
   __syncthreads();
 #pragma unroll 1
-  for (uint32_t d = 1; d < kRedThreads; d <<= 1) {
-    xyzt_t o;
-    const bool has = tid + d < kRedThreads;
-    if (has) xyzt_load(o, sh + (tid + d) * 12);
+  for (uint32_t d = 1; d < kRedQuads; d <<= 1) {
+    xyzt_t o = xyzt_identity();
+    if (q + d < kRedQuads) xyzt_load(o, sh + (q + d) * 12);
     __syncthreads();
-    if (has) {
-      X = te_add_ool(X, o);
-      xyzt_store(sh + tid * 12, X);
-    }
+    X = te_add_quad(X, o, kAllLanes);
+    if (ql == 0) xyzt_store(sh + q * 12, X);
     __syncthreads();
   }
   return X;
 }
 
-// Combine `cnt` runs (R, A) of 2^lin_log2 buckets each into one run (result in thread 0).
-// Thread t takes runs [t per, t per + per) (per a power of two) and forms SA = sum A_i,
-// RR = sum R_i and T = sum (i - t per) R_i.  Then
-//   A = sum_t SA_t + 2^lin_log2 (sum_t T_t + per sum_t t RR_t),  R = sum_t RR_t,
-// where sum_t t RR_t = sum_{t >= 1} (suffix sum of RR at t): one block scan and three block
-// sums, and only thread 0 doubles.
+// Combine `cnt` runs (R, A) of 2^lin_log2 buckets each into one run (result in quad 0).
+// Quad u takes runs [u per, u per + per) (per a power of two) and forms SA = sum A_i,
+// RR = sum R_i and T = sum (i - u per) R_i.  Then
+//   A = sum_u SA_u + 2^lin_log2 (sum_u T_u + per sum_u u RR_u),  R = sum_u RR_u,
+// where sum_u u RR_u = sum_{u >= 1} (suffix sum of RR at u): one block scan and three block
+// sums, and only quad 0 doubles.
 __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log2, bool want_r,
                               uint4 *sh, xyzt_t &A_out, xyzt_t &R_out) {
-  const uint32_t tid = threadIdx.x;
+  const uint32_t q = threadIdx.x >> 2;
   uint32_t per = 1, per_log2 = 0;
-  while (per * kRedThreads < cnt) {
+  while (per * kRedQuads < cnt) {
     per <<= 1;
     per_log2++;
   }
-  const uint32_t i0 = tid * per, i1 = min(i0 + per, cnt);
+  const uint32_t i0 = q * per;
   xyzt_t SA = xyzt_identity(), T = xyzt_identity(), RR = xyzt_identity();
 #pragma unroll 1
-  for (uint32_t i = i1; i-- > i0;) {
-    T = te_add_ool(T, RR);
-    xyzt_t R, A;
-    xyzt_load(R, items + (size_t)i * 24);
-    xyzt_load(A, items + (size_t)i * 24 + 12);
-    RR = te_add_ool(RR, R);
-    SA = te_add_ool(SA, A);
+  for (uint32_t k = per; k-- > 0;) {  // runs past cnt are the identity
+    const uint32_t i = i0 + k;
+    T = te_add_quad(T, RR, kAllLanes);
+    xyzt_t R = xyzt_identity(), A = xyzt_identity();
+    if (i < cnt) {
+      xyzt_load(R, items + (size_t)i * 24);
+      xyzt_load(A, items + (size_t)i * 24 + 12);
+    }
+    RR = te_add_quad(RR, R, kAllLanes);
+    SA = te_add_quad(SA, A, kAllLanes);
   }
   const xyzt_t suf = block_suffix_scan(RR, sh);
-  if (want_r && tid == 0) R_out = suf;  // suffix at 0 is the total
-  const xyzt_t sumY = block_sum(tid ? suf : xyzt_identity(), sh);
+  if (want_r && q == 0) R_out = suf;  // suffix at 0 is the total
+  const xyzt_t sumY = block_sum(q ? suf : xyzt_identity(), sh);
   const xyzt_t sumT = block_sum(T, sh);
   const xyzt_t sumSA = block_sum(SA, sh);
-  if (tid == 0) {
+  if (q == 0) {  // lanes 0..3 of warp 0
     xyzt_t X = sumY;
 #pragma unroll 1
-    for (uint32_t k = 0; k < per_log2; k++) X = te_dbl_ool(X);
-    X = te_add_ool(sumT, X);
+    for (uint32_t k = 0; k < per_log2; k++) X = te_dbl_quad(X, 0xfu);
+    X = te_add_quad(sumT, X, 0xfu);
 #pragma unroll 1
-    for (uint32_t k = 0; k < lin_log2; k++) X = te_dbl_ool(X);
-    A_out = te_add_ool(X, sumSA);
+    for (uint32_t k = 0; k < lin_log2; k++) X = te_dbl_quad(X, 0xfu);
+    A_out = te_add_quad(X, sumSA, 0xfu);
   }
 }
 
@@ -598,7 +664,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce2(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t g = blockIdx.x;
   if (g >= pb.n_grps) return;
-  __shared__ uint4 sh[kRedThreads * 12];
+  __shared__ uint4 sh[kRedQuads * 12];
   const WinDesc wd = pb.wins[find_win_grp(pb.wins, pb.n_wins, g)];
   const uint32_t G = 1u << pb.grp_len_log2;
   const uint32_t first = (g - wd.grp_begin) * G;
@@ -615,7 +681,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t gw = blockIdx.x;
   if (gw >= pb.n_wins) return;
-  __shared__ uint4 sh[kRedThreads * 12];
+  __shared__ uint4 sh[kRedQuads * 12];
   const WinDesc wd = pb.wins[gw];
   xyzt_t A, R;
   block_combine(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp, pb.red_len_log2 + pb.grp_len_log2,
@@ -630,61 +696,6 @@ __device__ __forceinline__ void load_class_point(wpt_t &p, const uint4 *cp) {
   fq_load(p.x, cp);
   fq_load(p.y, cp + 3);
   p.z = fq_one();
-}
-
-// ---- 4-lane cooperative point operations for the serial window combine ----
-// Lanes 0..3 (mask 0xf) hold the same point.  Each lane computes one of four independent
-// products and the lanes swap results, so a doubling costs two product latencies instead of
-// eight, and an addition three instead of nine.
-__device__ __forceinline__ fq_t shfl4(const fq_t &a, int src) {
-  fq_t r;
-#pragma unroll
-  for (int k = 0; k < FQ_LIMBS; k++) r.v[k] = __shfl_sync(0xfu, a.v[k], src, 4);
-  return r;
-}
-__device__ __forceinline__ fq_t pick4(int l, const fq_t &a, const fq_t &b, const fq_t &c, const fq_t &d) {
-  return fq_select(l == 0, a, fq_select(l == 1, b, fq_select(l == 2, c, d)));
-}
-
-__device__ __noinline__ xyzt_t te_dbl_quad(const xyzt_t &p) {
-  const int l = threadIdx.x & 3;
-  const fq_t sq = fq_sqr(pick4(l, p.x, p.y, p.z, fq_add(p.x, p.y)));
-  const fq_t A = shfl4(sq, 0), B = shfl4(sq, 1), ZZ = shfl4(sq, 2), S = shfl4(sq, 3);
-  const fq_t C = fq_dbl(ZZ);
-  const fq_t D = fq_neg(A);
-  const fq_t E = fq_sub(fq_sub(S, A), B);
-  const fq_t G = fq_add(D, B);
-  const fq_t F = fq_sub(G, C);
-  const fq_t H = fq_sub(D, B);
-  const fq_t pr = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
-  xyzt_t r;
-  r.x = shfl4(pr, 0);
-  r.y = shfl4(pr, 1);
-  r.t = shfl4(pr, 2);
-  r.z = shfl4(pr, 3);
-  return r;
-}
-
-__device__ __noinline__ xyzt_t te_add_quad(const xyzt_t &p, const xyzt_t &q) {
-  const uint32_t kc[FQ_LIMBS] = BLS_TE_K;
-  const int l = threadIdx.x & 3;
-  const fq_t m1 = pick4(l, fq_sub(p.y, p.x), fq_add(p.y, p.x), p.t, p.z);
-  const fq_t m2 = pick4(l, fq_sub(q.y, q.x), fq_add(q.y, q.x), q.t, q.z);
-  const fq_t pr = fq_mul(m1, m2);
-  const fq_t A = shfl4(pr, 0), B = shfl4(pr, 1), TT = shfl4(pr, 2), ZZ = shfl4(pr, 3);
-  const fq_t C = fq_mul(TT, fq_from(kc));
-  const fq_t D = fq_dbl(ZZ);
-  const fq_t E = fq_sub(B, A);
-  const fq_t F = fq_sub(D, C);
-  const fq_t G = fq_add(D, C);
-  const fq_t H = fq_add(B, A);
-  const fq_t pr2 = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
-  xyzt_t r;
-  r.x = shfl4(pr2, 0);
-  r.y = shfl4(pr2, 1);
-  r.t = shfl4(pr2, 2);
-  r.z = shfl4(pr2, 3);
-  return r;
 }
 
 __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
@@ -717,10 +728,10 @@ __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
 #pragma unroll 1
     for (int w = (int)jd.nred - 2; w >= 0; w--) {
 #pragma unroll 1
-      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_quad(acc);
+      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_quad(acc, 0xfu);
       xyzt_t ws;
       xyzt_load(ws, pb.win_sum + (size_t)(jd.win_begin + w) * 12);
-      acc = te_add_quad(acc, ws);
+      acc = te_add_quad(acc, ws, 0xfu);
     }
   }
   if (threadIdx.x != 0) return;
