@@ -66,6 +66,9 @@ enum : int {
   CNT_WORDS = 8,
 };
 
+#define MSM_POINTS_PER_CHUNK 256  // points per histogram block (one chunk of the stage)
+#define MSM_MAX_BINS 32           // key ranges of the staged sort
+
 // Everything a pass needs on the device; sized by the host (msm_plan_pass).
 struct PassBuffers {
   const uint4 *bases;           // resident bases, 9 x uint4 each
@@ -93,6 +96,16 @@ struct PassBuffers {
   uint32_t n_grps;              // level-2 groups
   uint64_t max_entries;         // capacity of vals
   uint32_t max_tasks;           // capacity of tasks / partials
+
+  // staged sort (or stage == null: the scatter re-reads the scalars once per key range).
+  // k_count writes the entries of its 256 points, (key, base index | sign << 31), into the
+  // block's chunk of `stage`, grouped by key range (key >> bin_shift); blk_off holds each
+  // chunk's n_bins + 1 range starts.  The scatter then reads one key range per launch.
+  uint2 *stage;                 // [n_chunks * stage_cap]
+  uint32_t *blk_off;            // [n_chunks * (n_bins + 1)]
+  uint32_t stage_cap;           // entries per chunk: 256 x the pass's largest window count
+  uint32_t bin_shift;           // key range of a bucket key
+  uint32_t n_bins;              // key ranges (<= MSM_MAX_BINS)
 
   uint32_t *count;              // [n_buckets]
   uint32_t *offset;             // [n_buckets]
@@ -123,6 +136,8 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t str
 #define MSM_NUM_STAGES 10
 size_t msm_scan_tmp_words(uint32_t n_buckets);
 uint32_t msm_scatter_passes(uint64_t max_entries);
+uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries);
+uint64_t msm_upload_chunk_points(uint64_t n_points, int nchunks);
 
 // resident-base preparation
 cudaError_t msm_launch_precompute(const void *d_affine, size_t n, uint4 *d_bases, uint8_t *d_flags,

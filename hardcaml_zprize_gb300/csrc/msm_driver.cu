@@ -215,6 +215,10 @@ struct Plan {
   uint64_t n_points = 0, max_entries = 0;
   uint32_t n_buckets = 0, n_segs = 0, n_grps = 0, max_tasks = 0;
   uint32_t seg_len = 1024, red_log2 = 5;
+  // staged sort: histogram chunks of MSM_POINTS_PER_CHUNK points, each with room for the
+  // largest window count of the pass, and the key ranges of the scatter
+  uint64_t n_chunks = 0;
+  uint32_t stage_cap = 0, bin_shift = 0, n_bins = 0;
   std::string key;
 };
 
@@ -276,6 +280,13 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
     return fail(ERR_BUDGET, "pass too large: %llu buckets, %llu entries",
                 (unsigned long long)buckets, (unsigned long long)pl.max_entries);
   pl.n_buckets = (uint32_t)buckets;
+  uint32_t max_nwin = 0;
+  for (const JobDesc &d : pl.jobs) max_nwin = std::max(max_nwin, d.nwin);
+  pl.n_chunks = (pl.n_points + MSM_POINTS_PER_CHUNK - 1) / MSM_POINTS_PER_CHUNK;
+  pl.stage_cap = MSM_POINTS_PER_CHUNK * max_nwin;
+  pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries);
+  pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
+  if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
   pl.n_segs = (uint32_t)segs;
   pl.n_grps = (uint32_t)grps;
   const uint64_t mt = buckets + pl.max_entries / pl.seg_len + 1;
@@ -291,6 +302,7 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
   uint64_t b = 0;
   b += (uint64_t)pl.n_buckets * 4 * 5;                   // count, offset, fill, taskoff, heavy
   b += pl.max_entries * 4;                                // vals
+  b += pl.n_chunks * ((uint64_t)pl.stage_cap * 8 + (pl.n_bins + 1) * 4);  // stage, blk_off
   b += (uint64_t)pl.max_tasks * (sizeof(Task) + 4 + MSM_BUCKET_BYTES);
   b += (uint64_t)(pl.n_segs + pl.n_grps) * 2 * MSM_BUCKET_BYTES;
   b += (uint64_t)pl.wins.size() * MSM_BUCKET_BYTES;
@@ -304,7 +316,7 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
 // ---------------------------------------------------------------------------------------------
 struct Workspace {
   DevBuf count, offset, fill, taskoff, scan_tmp, vals, tasks, partials, heavy, counters, seg_out,
-      grp_out, win_sum, results, jobs, wins, order, len_hist;
+      grp_out, win_sum, results, jobs, wins, order, len_hist, stage, blk_off;
   DevBuf scalars[2];
   HostPinned res_host;
   cudaEvent_t ev[MSM_NUM_STAGES + 1] = {};
@@ -329,6 +341,8 @@ struct Workspace {
     CK(heavy.ensure((size_t)pl.n_buckets * 4, &moved));
     CK(scan_tmp.ensure(msm_scan_tmp_words(pl.n_buckets) * 4, &moved));
     CK(vals.ensure((size_t)pl.max_entries * 4, &moved));
+    CK(stage.ensure((size_t)pl.n_chunks * pl.stage_cap * 8, &moved));
+    CK(blk_off.ensure((size_t)pl.n_chunks * (pl.n_bins + 1) * 4, &moved));
     CK(tasks.ensure((size_t)pl.max_tasks * sizeof(Task), &moved));
     CK(partials.ensure((size_t)pl.max_tasks * MSM_BUCKET_BYTES, &moved));
     CK(order.ensure((size_t)pl.max_tasks * 4, &moved));
@@ -355,6 +369,7 @@ struct Workspace {
     graphs.clear();
     count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
     scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
+    stage.release(); blk_off.release();
     order.release(); len_hist.release(); grp_out.release();
     win_sum.release(); scalars[0].release(); scalars[1].release();
     generation++;
@@ -426,6 +441,11 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.taskoff = ws.taskoff.as<uint32_t>();
   pb.scan_tmp = ws.scan_tmp.as<uint32_t>();
   pb.vals = ws.vals.as<uint32_t>();
+  pb.stage = pl.n_chunks ? ws.stage.as<uint2>() : nullptr;
+  pb.blk_off = ws.blk_off.as<uint32_t>();
+  pb.stage_cap = pl.stage_cap;
+  pb.bin_shift = pl.bin_shift;
+  pb.n_bins = pl.n_bins;
   pb.tasks = ws.tasks.as<Task>();
   pb.partials = ws.partials.as<uint4>();
   pb.heavy = ws.heavy.as<uint32_t>();
@@ -634,8 +654,9 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     if (build_plan(one, pl)) return g_err;
     const void *src = d_scalars, *pull = nullptr;
     const cudaEvent_t *chunks = nullptr;
-    if (!src && host_pullable(cx, h_scalars + first[j])) {
-      // the histogram kernel reads the scalars from host memory and leaves the device copy
+    if (!src && j == 0 && host_pullable(cx, h_scalars + first[j])) {
+      // the first MSM's histogram kernel reads its scalars from host memory and leaves the
+      // device copy; later MSMs' scalars are copied while the previous pass computes
       src = ws.scalars[(int)(j & 1)].p;
       pull = h_scalars + first[j];
     } else if (!src) {
@@ -643,7 +664,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
       const int slot = (int)(j & 1);
       const int nch = Ctx::kCopyChunks;
       CK(cudaStreamWaitEvent(cx->copy_stream, cx->freed[slot], 0));
-      const uint64_t per = (sizes[j] + nch - 1) / nch;
+      const uint64_t per = msm_upload_chunk_points(sizes[j], nch);
       for (int c = 0; c < nch; c++) {
         const uint64_t a = std::min<uint64_t>((uint64_t)c * per, sizes[j]);
         const uint64_t b = std::min<uint64_t>(a + per, sizes[j]);

@@ -87,7 +87,9 @@ __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, ui
 // ---------------------------------------------------------------------------------------------
 // 1. histogram
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s) {
+// Round 1: the global bucket histogram (and, for the staged sort, the block's key-range counts).
+__device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s,
+                                             uint32_t *sh_bins) {
   uint32_t carry = 0;
   for (uint32_t w = 0; w < jd.nwin; w++) {
     const int32_t d = next_digit(s, jd, w, carry);
@@ -103,29 +105,85 @@ __device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDes
     } else {
       atomicAdd(&pb.count[key], 1u);
     }
+    if (sh_bins) atomicAdd(&sh_bins[key >> pb.bin_shift], 1u);
   }
 }
 
-__global__ void k_count(PassBuffers pb, uint64_t g_begin, uint64_t g_end) {
-  const uint64_t g = g_begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= g_end || g >= pb.n_points) return;
-  const uint32_t j = find_job(pb.jobs, pb.n_jobs, g);
-  const JobDesc jd = pb.jobs[j];
-  const uint64_t i = g - jd.point_begin;
-  const uint64_t si = 2 * (jd.scalar_off + i);
-  if (pb.host_scalars) {
-    // fused upload: every scalar of the pass (bases without a bucket entry included, k_final
-    // reads theirs) goes from host memory to the device copy the later kernels read
-    const uint4 a = pb.host_scalars[si], b = pb.host_scalars[si + 1];
-    uint4 *dst = const_cast<uint4 *>(pb.scalars) + si;
-    dst[0] = a;
-    dst[1] = b;
-    if (pb.flags[jd.base_off + i] != BASE_OK) return;
-    count_digits(pb, jd, scalar_bits(a, b));
-  } else {
-    if (pb.flags[jd.base_off + i] != BASE_OK) return;
-    count_digits(pb, jd, load_scalar(pb.scalars + si));
+// Round 2 of the staged sort: the entries of one point into the block's chunk, at the cursors
+// of their key ranges.
+__device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s,
+                                             uint64_t bidx, uint32_t *sh_cur, uint2 *chunk) {
+  uint32_t carry = 0;
+  for (uint32_t w = 0; w < jd.nwin; w++) {
+    const int32_t d = next_digit(s, jd, w, carry);
+    if (d == 0) continue;
+    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
+    const uint32_t val = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
+    const uint32_t pos = atomicAdd(&sh_cur[key >> pb.bin_shift], 1u);
+    if (pos < pb.stage_cap) {
+      chunk[pos] = make_uint2(key, val);
+    } else {
+      set_error(pb.counters, 6, pos);
+    }
   }
+}
+
+// One thread per point, 256 points per block.  With host_scalars set, the kernel also uploads
+// the pass's scalars; with stage set, the block also writes its entries to its chunk of the
+// stage, grouped by key range.
+__global__ void __launch_bounds__(MSM_POINTS_PER_CHUNK) k_count(PassBuffers pb, uint64_t g_begin,
+                                                                uint64_t g_end) {
+  __shared__ uint32_t sh_cur[MSM_MAX_BINS];
+  const uint32_t tid = threadIdx.x;
+  const bool staged = pb.stage != nullptr;
+  const uint64_t g = g_begin + (uint64_t)blockIdx.x * blockDim.x + tid;
+  bool ok = false;
+  JobDesc jd{};
+  ScalarBits s{};
+  uint64_t bidx = 0;
+  if (g < g_end && g < pb.n_points) {
+    jd = pb.jobs[find_job(pb.jobs, pb.n_jobs, g)];
+    const uint64_t i = g - jd.point_begin;
+    const uint64_t si = 2 * (jd.scalar_off + i);
+    uint4 a, b;
+    if (pb.host_scalars) {
+      // fused upload: every scalar of the pass (bases without a bucket entry included, k_final
+      // reads theirs) goes from host memory to the device copy the later kernels read
+      a = pb.host_scalars[si];
+      b = pb.host_scalars[si + 1];
+      uint4 *dst = const_cast<uint4 *>(pb.scalars) + si;
+      dst[0] = a;
+      dst[1] = b;
+    } else {
+      a = pb.scalars[si];
+      b = pb.scalars[si + 1];
+    }
+    bidx = jd.base_off + i;
+    ok = pb.flags[bidx] == BASE_OK;
+    s = scalar_bits(a, b);
+  }
+  if (staged) {
+    if (tid < MSM_MAX_BINS) sh_cur[tid] = 0;
+    __syncthreads();
+  }
+  if (ok) count_digits(pb, jd, s, staged ? sh_cur : nullptr);
+  if (!staged) return;
+  __syncthreads();
+  const uint64_t chunk = g_begin / MSM_POINTS_PER_CHUNK + blockIdx.x;
+  if (tid == 0) {  // key-range counts -> starts (n_bins <= 32)
+    uint32_t *bo = pb.blk_off + chunk * (pb.n_bins + 1);
+    uint32_t acc = 0;
+    for (uint32_t r = 0; r < pb.n_bins; r++) {
+      const uint32_t c = sh_cur[r];
+      sh_cur[r] = acc;
+      bo[r] = acc;
+      acc += c;
+    }
+    bo[pb.n_bins] = acc;
+  }
+  __syncthreads();
+  if (ok) stage_digits(pb, jd, s, bidx, sh_cur, pb.stage + chunk * pb.stage_cap);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -305,6 +363,41 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
       } else {
         set_error(pb.counters, 3, pos[k]);
       }
+    }
+  }
+}
+
+// Staged sort: the entries of key range `bin`, chunk by chunk (one block per histogram block),
+// each to the position its bucket's slot cursor returns.  The range's slice of the sorted array
+// stays in L2 while the launch runs.
+__global__ void __launch_bounds__(256) k_scatter_staged(PassBuffers pb, uint32_t bin) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint64_t chunk = blockIdx.x;
+  const uint32_t *bo = pb.blk_off + chunk * (pb.n_bins + 1);
+  const uint32_t lo = bo[bin], hi = min(bo[bin + 1], pb.stage_cap);
+  const uint2 *st = pb.stage + chunk * pb.stage_cap;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+    const uint2 kv = st[e];
+    if (kv.x >= pb.n_buckets) {  // cannot happen for a consistent stage; never write out of bounds
+      set_error(pb.counters, 7, kv.x);
+      continue;
+    }
+    uint32_t pos;
+    const uint32_t active = __activemask();
+    const int leader = __ffs(active) - 1;
+    const uint32_t k0 = __shfl_sync(active, kv.x, leader);
+    if (__all_sync(active, kv.x == k0)) {  // one bucket for the whole warp: one atomic
+      uint32_t bp = 0;
+      if (lane == leader) bp = atomicAdd(&pb.fill[kv.x], (uint32_t)__popc(active));
+      pos = __shfl_sync(active, bp, leader) + __popc(active & ((1u << lane) - 1u));
+    } else {
+      pos = atomicAdd(&pb.fill[kv.x], 1u);
+    }
+    if (pos < pb.max_entries) {
+      pb.vals[pos] = kv.y;
+    } else {
+      set_error(pb.counters, 3, pos);
     }
   }
 }
@@ -769,6 +862,24 @@ uint32_t msm_scatter_passes(uint64_t max_entries) {
   return (uint32_t)(p < 1 ? 1 : p > 8 ? 8 : p);
 }
 
+// Key ranges of the staged sort: one per ~150 MB of sorted array, as a shift of the bucket key
+// (ranges of 2^shift keys, at most MSM_MAX_BINS of them).  On GB300 the best counts measured
+// were 4 ranges for 2^24 points x 12 windows and 16 for 2^26 x 11 windows.
+uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries) {
+  const uint64_t per = 150ull << 20, want = (max_entries * 4 + per / 2) / per;
+  const uint32_t target = (uint32_t)(want < 1 ? 1 : want > MSM_MAX_BINS ? MSM_MAX_BINS : want);
+  uint32_t shift = 0;
+  while (shift < 31 && (((uint64_t)n_buckets + (1ull << shift) - 1) >> shift) > target) shift++;
+  return shift;
+}
+
+// Points per chunk of a chunked scalar upload: a multiple of the histogram block, so every block
+// of a chunk's histogram launch is a whole chunk of the stage.
+uint64_t msm_upload_chunk_points(uint64_t n_points, int nchunks) {
+  const uint64_t per = (n_points + nchunks - 1) / nchunks;
+  return (per + MSM_POINTS_PER_CHUNK - 1) / MSM_POINTS_PER_CHUNK * MSM_POINTS_PER_CHUNK;
+}
+
 size_t msm_scan_tmp_words(uint32_t n_buckets) {
   return 2ull * ((n_buckets + kScanBlock - 1) / kScanBlock) + 2;
 }
@@ -788,7 +899,7 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   if (pb.n_points > 0) {
     if (chunk_ready && nchunks > 0) {
       // the scalars arrive in chunks on another stream: count each chunk as soon as it lands
-      const uint64_t per = (pb.n_points + nchunks - 1) / nchunks;
+      const uint64_t per = msm_upload_chunk_points(pb.n_points, nchunks);
       for (int c = 0; c < nchunks; c++) {
         const uint64_t g0 = (uint64_t)c * per, g1 = g0 + per < pb.n_points ? g0 + per : pb.n_points;
         if ((e = cudaStreamWaitEvent(st, chunk_ready[c], 0))) return e;
@@ -813,7 +924,12 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
     launched++;
   }
   mark(2);
-  if (pb.n_points > 0) {
+  if (pb.n_points > 0 && pb.stage) {
+    for (uint32_t r = 0; r < pb.n_bins; r++) {
+      k_scatter_staged<<<pts_blocks, 256, 0, st>>>(pb, r);
+      launched++;
+    }
+  } else if (pb.n_points > 0) {
     const uint32_t passes = msm_scatter_passes(pb.max_entries);
     for (uint32_t p = 0; p < passes; p++) {
       const uint32_t lo = (uint32_t)((uint64_t)pb.n_buckets * p / passes);
