@@ -284,9 +284,13 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   for (const JobDesc &d : pl.jobs) max_nwin = std::max(max_nwin, d.nwin);
   pl.n_chunks = (pl.n_points + MSM_POINTS_PER_CHUNK - 1) / MSM_POINTS_PER_CHUNK;
   pl.stage_cap = MSM_POINTS_PER_CHUNK * max_nwin;
-  pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries);
+  // MSM_SORT_RANGES=<n> overrides the number of key ranges of the staged sort (tests, tuning)
+  const char *sr = getenv("MSM_SORT_RANGES");
+  pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u);
   pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
   if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
+  snprintf(tmp, sizeof(tmp), "|r%u", pl.bin_shift);
+  pl.key += tmp;
   pl.n_segs = (uint32_t)segs;
   pl.n_grps = (uint32_t)grps;
   const uint64_t mt = buckets + pl.max_entries / pl.seg_len + 1;

@@ -865,8 +865,10 @@ uint32_t msm_scatter_passes(uint64_t max_entries) {
 // Key ranges of the staged sort: one per ~150 MB of sorted array, as a shift of the bucket key
 // (ranges of 2^shift keys, at most MSM_MAX_BINS of them).  On GB300 the best counts measured
 // were 4 ranges for 2^24 points x 12 windows and 16 for 2^26 x 11 windows.
-uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries) {
-  const uint64_t per = 150ull << 20, want = (max_entries * 4 + per / 2) / per;
+// `ranges` > 0 asks for that many ranges instead (rounded to a shift).
+uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries, uint32_t ranges) {
+  const uint64_t per = 150ull << 20;
+  const uint64_t want = ranges ? ranges : (max_entries * 4 + per / 2) / per;
   const uint32_t target = (uint32_t)(want < 1 ? 1 : want > MSM_MAX_BINS ? MSM_MAX_BINS : want);
   uint32_t shift = 0;
   while (shift < 31 && (((uint64_t)n_buckets + (1ull << shift) - 1) >> shift) > target) shift++;

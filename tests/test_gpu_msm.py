@@ -384,6 +384,31 @@ def test_fixed_base_parity(engine, ref, ocpu, kats):
         ctx.close()
 
 
+@pytest.mark.parametrize("ranges", [3, 8, 32])
+def test_staged_sort_key_ranges(engine, ocpu, monkeypatch, ranges):
+    """The staged sort with several key ranges (one scatter launch each), which the default rule
+    uses only for sorted arrays of hundreds of MB: windowed and fixed-base MSMs, uniform scalars,
+    the uneven-batch mix (16-bit values, 0 and r-1, one repeated value) and all-equal scalars."""
+    nb = 1 << 13
+    pts = ocpu.gen_bases(909, nb)
+    sizes = [nb, 3000, 1, 4096]
+    offs = [0, 17, 100, 4000]
+    sc = np.concatenate([engine.generate_scalars(910, nb), engine.generate_scalars(911, 3000, kind=1),
+                         engine.generate_scalars(912, 1),
+                         np.repeat(engine.generate_scalars(913, 1), 4096, axis=0)])
+    first = np.concatenate([[0], np.cumsum(sizes)])
+    want = [ocpu.msm(pts[o:o + s], sc[first[j]:first[j] + s]) for j, (s, o) in enumerate(zip(sizes, offs))]
+    monkeypatch.setenv("MSM_SORT_RANGES", str(ranges))
+    for ctx in (engine.multi_scalar_mult_init(pts), _ctx_with_fixed_base(engine, pts, 12)):
+        try:
+            for opts in (dict(mode=1), dict(mode=2), dict(mode=2, use_graph=1), dict(fixed_base=1, mode=1)):
+                out = ctx.mult_uneven(sizes, offs, sc, **opts)
+                for j in range(len(sizes)):
+                    assert np.array_equal(out[j], want[j]), (ranges, opts, j)
+        finally:
+            ctx.close()
+
+
 def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
     """The reference's second edge case holds a representable base of order 4, whose doubling
     chain reaches the order-two point (0, -1) and then the identity; the tables stay exact.  (A
