@@ -5,7 +5,8 @@
 //   3. k_scatter   counting-sort scatter of (base index | sign) into bucket order
 //   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
 //   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
-//   6. k_merge     buckets split over several runs: warp-parallel sum of their partials
+//   6. k_merge_*   buckets split over several runs: sum of their partials (a thread per bucket
+//                  of a few runs, a warp per bucket of many)
 //   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33)
 //   8. k_reduce2/3 combine runs into groups, groups into window sums
 //   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
@@ -530,6 +531,31 @@ __device__ __forceinline__ xyzt_t warp_sum_xyzt(xyzt_t acc) {
   return acc;
 }
 
+// Split buckets of at most kMergeThreadMax runs (the common case: a few more entries than
+// seg_len) are summed by one thread each, the rest by one warp each (k_merge).  Lanes of a warp
+// execute one instruction stream, so a warp's tree over three partials costs as much as the
+// thread version summing 32 such buckets.
+constexpr uint32_t kMergeThreadMax = 16;
+
+__global__ void __launch_bounds__(128) k_merge_small(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t nheavy = pb.counters[CNT_HEAVY];
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nheavy; h += gridDim.x * blockDim.x) {
+    const uint32_t b = pb.heavy[h];
+    const uint32_t nt = ntask_of(pb.count[b], pb.seg_len);
+    if (nt > kMergeThreadMax) continue;
+    const uint32_t t0 = pb.taskoff[b];
+    xyzt_t acc;
+    xyzt_load(acc, pb.partials + (size_t)t0 * 12);
+    for (uint32_t k = 1; k < nt; k++) {
+      xyzt_t p;
+      xyzt_load(p, pb.partials + (size_t)(t0 + k) * 12);
+      acc = te_add_ool(acc, p);
+    }
+    xyzt_store(pb.partials + (size_t)t0 * 12, acc);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const int lane = threadIdx.x & 31;
@@ -539,6 +565,7 @@ __global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
   for (uint32_t h = warp_global; h < nheavy; h += nwarps) {
     const uint32_t b = pb.heavy[h];
     const uint32_t nt = ntask_of(pb.count[b], pb.seg_len);
+    if (nt <= kMergeThreadMax) continue;  // k_merge_small's
     const uint32_t t0 = pb.taskoff[b];
     xyzt_t acc = xyzt_identity();
     for (uint32_t k = lane; k < nt; k += 32) {
@@ -672,24 +699,35 @@ constexpr uint32_t kAllLanes = 0xffffffffu;
 // block executes every addition (a quad with nothing to add adds the identity), which keeps the
 // warps converged for the quad shuffles.
 
-// Sum over the block's quads in shared memory; the result is valid in quad 0.  At each level
-// only the warps holding a quad below the stride add (whole warps, so their shuffles stay
-// converged).
-__device__ __forceinline__ xyzt_t block_sum(xyzt_t X, uint4 *sh) {
+// Three independent sums over the block's quads at once (sh holds 3 x kRedQuads points): at
+// each tree level the 3 x stride additions are spread over the quads, so the three trees take 7
+// rounds of dependent additions instead of 18.  Only warps holding an active quad add (whole
+// warps, so their shuffles stay converged).  The sums are valid in quad 0.
+__device__ __forceinline__ void block_sum3(xyzt_t (&X)[3], uint4 *sh) {
   const uint32_t q = threadIdx.x >> 2, ql = threadIdx.x & 3;
   const uint32_t warp_q0 = (threadIdx.x >> 5) * 8;  // first quad of this warp
-  if (ql == 0) xyzt_store(sh + q * 12, X);
+  if (ql == 0)
+    for (int k = 0; k < 3; k++) xyzt_store(sh + (k * kRedQuads + q) * 12, X[k]);
   __syncthreads();
 #pragma unroll 1
   for (uint32_t stride = kRedQuads / 2; stride > 0; stride >>= 1) {
-    xyzt_t o = xyzt_identity();
-    if (q < stride) xyzt_load(o, sh + (q + stride) * 12);
-    if (warp_q0 < stride) X = te_add_quad(X, o, kAllLanes);
-    __syncthreads();
-    if (q < stride && ql == 0) xyzt_store(sh + q * 12, X);
-    __syncthreads();
+#pragma unroll 1
+    for (uint32_t u0 = 0; u0 < 3 * stride; u0 += kRedQuads) {
+      const uint32_t u = u0 + q;  // item u: array u / stride, element u % stride
+      const bool act = u < 3 * stride;
+      const uint32_t slot = act ? (u / stride) * kRedQuads + u % stride : 0;
+      xyzt_t a = xyzt_identity(), o = xyzt_identity();
+      if (act) {
+        xyzt_load(a, sh + slot * 12);
+        xyzt_load(o, sh + (slot + stride) * 12);
+      }
+      if (u0 + warp_q0 < 3 * stride) a = te_add_quad(a, o, kAllLanes);
+      __syncthreads();
+      if (act && ql == 0) xyzt_store(sh + slot * 12, a);
+      __syncthreads();
+    }
   }
-  return X;
+  for (int k = 0; k < 3; k++) xyzt_load(X[k], sh + k * kRedQuads * 12);
 }
 
 // Inclusive suffix sums over the quads: quad u gets sum_{v >= u} X_v (Hillis-Steele).
@@ -714,7 +752,7 @@ __device__ __forceinline__ xyzt_t block_suffix_scan(xyzt_t X, uint4 *sh) {
 // RR = sum R_i and T = sum (i - u per) R_i.  Then
 //   A = sum_u SA_u + 2^lin_log2 (sum_u T_u + per sum_u u RR_u),  R = sum_u RR_u,
 // where sum_u u RR_u = sum_{u >= 1} (suffix sum of RR at u): one block scan and three block
-// sums, and only quad 0 doubles.
+// sums (run together), and only quad 0 doubles.
 __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log2, bool want_r,
                               uint4 *sh, xyzt_t &A_out, xyzt_t &R_out) {
   const uint32_t q = threadIdx.x >> 2;
@@ -739,11 +777,11 @@ __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log
   }
   const xyzt_t suf = block_suffix_scan(RR, sh);
   if (want_r && q == 0) R_out = suf;  // suffix at 0 is the total
-  const xyzt_t sumY = block_sum(q ? suf : xyzt_identity(), sh);
-  const xyzt_t sumT = block_sum(T, sh);
-  const xyzt_t sumSA = block_sum(SA, sh);
+  xyzt_t S[3] = {q ? suf : xyzt_identity(), T, SA};
+  block_sum3(S, sh);
+  const xyzt_t &sumT = S[1], &sumSA = S[2];
   if (q == 0) {  // lanes 0..3 of warp 0
-    xyzt_t X = sumY;
+    xyzt_t X = S[0];
 #pragma unroll 1
     for (uint32_t k = 0; k < per_log2; k++) X = te_dbl_quad(X, 0xfu);
     X = te_add_quad(sumT, X, 0xfu);
@@ -757,7 +795,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce2(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t g = blockIdx.x;
   if (g >= pb.n_grps) return;
-  __shared__ uint4 sh[kRedQuads * 12];
+  __shared__ uint4 sh[3 * kRedQuads * 12];
   const WinDesc wd = pb.wins[find_win_grp(pb.wins, pb.n_wins, g)];
   const uint32_t G = 1u << pb.grp_len_log2;
   const uint32_t first = (g - wd.grp_begin) * G;
@@ -774,7 +812,7 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t gw = blockIdx.x;
   if (gw >= pb.n_wins) return;
-  __shared__ uint4 sh[kRedQuads * 12];
+  __shared__ uint4 sh[3 * kRedQuads * 12];
   const WinDesc wd = pb.wins[gw];
   xyzt_t A, R;
   block_combine(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp, pb.red_len_log2 + pb.grp_len_log2,
@@ -953,6 +991,8 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   k_accumulate<<<num_sms * 4, 128, 0, st>>>(pb);
   launched++;
   mark(5);
+  k_merge_small<<<num_sms * 4, 128, 0, st>>>(pb);
+  launched++;
   k_merge<<<num_sms, 256, 0, st>>>(pb);
   launched++;
   mark(6);
