@@ -273,7 +273,9 @@ def run_ours(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
         "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n,
-                   "l2": "inputs larger than L2 (512 MB scalars, 2.4 GB bases)",
+                   "l2": f"inputs larger than L2 ({n * 32 / 2**20:.0f} MB scalars, "
+                         f"{n * 144 / 2**30:.2f} GB bases"
+                         + (f", {n * w_used * 144 / 2**30:.1f} GB fixed-base tables)" if cfg["fixed_base"] == 1 else ")"),
                    "window_bits": cfg["window_bits"], "signed_digits": cfg["signed_digits"] == 1,
                    "seg_len": cfg["seg_len"], "red_len_log2": cfg["red_len_log2"],
                    "fixed_base_tables": cfg["fixed_base"] == 1},
@@ -296,6 +298,13 @@ def run_ours(args, rank, world, local):
             "msm_frac": algorithmic_imad(n) / msm_s / peak_imad,
         },
         "stages_ms": stage_acc,
+        # achieved HBM rates of the two input streams: k_accumulate reads a 144 B base (table
+        # entry) and a 4 B sorted entry per point and window; k_count reads the 32 B scalars
+        "streams_gbs": {
+            "bases_in_accumulate": n * w_used * 148 / t_acc / 1e9 if t_acc > 0 else None,
+            "scalars_in_count": n * 32 / (stage_acc.get("count", 0) * 1e-3) / 1e9
+            if stage_acc.get("count", 0) > 0 else None,
+        },
         "pass_stats": stats,
         "clocks": clocks,
         "device": info,
