@@ -5,8 +5,8 @@
 //   3. k_scatter   counting-sort scatter of (base index | sign) into bucket order
 //   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
 //   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
-//   6. k_merge_*   buckets split over several runs: sum of their partials (a thread per bucket
-//                  of a few runs, a warp per bucket of many)
+//   6. k_merge_*   buckets split over several runs: sum of their partials (a thread, a warp or
+//                  a block per bucket, by the number of runs)
 //   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33)
 //   8. k_reduce2/3 combine runs into groups, groups into window sums
 //   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
@@ -532,7 +532,8 @@ __device__ __forceinline__ xyzt_t warp_sum_xyzt(xyzt_t acc) {
 }
 
 // Split buckets of at most kMergeThreadMax runs (the common case: a few more entries than
-// seg_len) are summed by one thread each, the rest by one warp each (k_merge).  Lanes of a warp
+// seg_len) are summed by one thread each, larger ones by a warp (k_merge) or a block
+// (k_merge_big).  Lanes of a warp
 // execute one instruction stream, so a warp's tree over three partials costs as much as the
 // thread version summing 32 such buckets.
 constexpr uint32_t kMergeThreadMax = 16;
@@ -556,6 +557,10 @@ __global__ void __launch_bounds__(128) k_merge_small(PassBuffers pb) {
   }
 }
 
+// Buckets of more than kMergeWarpMax runs (a value repeated across many scalars) get a block of
+// 64 quads each (k_merge_big, after the quad arithmetic below).
+constexpr uint32_t kMergeWarpMax = 64;
+
 __global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const int lane = threadIdx.x & 31;
@@ -565,7 +570,7 @@ __global__ void __launch_bounds__(256) k_merge(PassBuffers pb) {
   for (uint32_t h = warp_global; h < nheavy; h += nwarps) {
     const uint32_t b = pb.heavy[h];
     const uint32_t nt = ntask_of(pb.count[b], pb.seg_len);
-    if (nt <= kMergeThreadMax) continue;  // k_merge_small's
+    if (nt <= kMergeThreadMax || nt > kMergeWarpMax) continue;  // k_merge_small's, k_merge_big's
     const uint32_t t0 = pb.taskoff[b];
     xyzt_t acc = xyzt_identity();
     for (uint32_t k = lane; k < nt; k += 32) {
@@ -635,60 +640,76 @@ __global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
   xyzt_store(pb.seg_out + (size_t)s * 24 + 12, A);
 }
 
-// ---- 4-lane cooperative point operations ----
-// The four lanes of a quad (lanes 4k..4k+3 of a warp) hold the same point.  Each lane computes one
-// of four independent products and the lanes swap results, so a doubling costs two product
-// latencies instead of eight and an addition three instead of nine.  `mask` names the lanes
-// executing the call (whole quads).
-__device__ __forceinline__ fq_t shfl4(const fq_t &a, int src, uint32_t mask) {
+// ---- 4-lane cooperative point operations on distributed points ----
+// The four lanes of a quad (lanes 4k..4k+3 of a warp) hold one extended point, one coordinate
+// each: lane 0 X, lane 1 T, lane 2 Y, lane 3 Z.  Each lane computes one of the four independent
+// products of a step and the lanes exchange what the next step needs, so a doubling costs two
+// product latencies instead of eight and an addition three instead of nine, and a point takes 12
+// registers per lane.  `mask` names the lanes executing the call (whole quads).
+__device__ __forceinline__ int dq_lane() { return (int)(threadIdx.x & 3); }
+
+// offset (uint4) of this lane's coordinate in an (X, Y, Z, T) record of 12 uint4
+__device__ __forceinline__ int dq_off() {
+  const int l = dq_lane();
+  return l == 0 ? 0 : l == 1 ? 9 : l == 2 ? 3 : 6;
+}
+__device__ __forceinline__ fq_t dq_load(const uint4 *p) {
+  fq_t r;
+  fq_load(r, p + dq_off());
+  return r;
+}
+__device__ __forceinline__ void dq_store(uint4 *p, const fq_t &v) { fq_store(p + dq_off(), v); }
+__device__ __forceinline__ fq_t dq_identity() { return dq_lane() >= 2 ? fq_one() : fq_zero(); }
+
+// the value of lane (this lane ^ x) of the quad
+__device__ __forceinline__ fq_t dq_xchg(const fq_t &a, int x, uint32_t mask) {
   fq_t r;
 #pragma unroll
-  for (int k = 0; k < FQ_LIMBS; k++) r.v[k] = __shfl_sync(mask, a.v[k], src, 4);
+  for (int k = 0; k < FQ_LIMBS; k++) r.v[k] = __shfl_xor_sync(mask, a.v[k], x, 4);
   return r;
 }
 __device__ __forceinline__ fq_t pick4(int l, const fq_t &a, const fq_t &b, const fq_t &c, const fq_t &d) {
   return fq_select(l == 0, a, fq_select(l == 1, b, fq_select(l == 2, c, d)));
 }
 
-__device__ __noinline__ xyzt_t te_dbl_quad(const xyzt_t &p, uint32_t mask) {
-  const int l = threadIdx.x & 3;
-  const fq_t sq = fq_sqr(pick4(l, p.x, p.y, p.z, fq_add(p.x, p.y)));
-  const fq_t A = shfl4(sq, 0, mask), B = shfl4(sq, 1, mask), ZZ = shfl4(sq, 2, mask), S = shfl4(sq, 3, mask);
+// dbl-2008-hwcd, a = -1: A = X^2, B = Y^2, C = 2 Z^2, S = (X + Y)^2, E = S - A - B, G = B - A,
+// F = G - C, H = -A - B; X3 = E F, Y3 = G H, T3 = E H, Z3 = F G
+static __device__ __noinline__ fq_t dq_dbl(fq_t p, uint32_t mask) {
+  const int l = dq_lane();
+  const fq_t o1 = dq_xchg(p, 1, mask), o3 = dq_xchg(p, 3, mask);  // lane 1 gets X and Y
+  const fq_t sq = fq_sqr(l == 1 ? fq_add(o1, o3) : p);              // A, S, B, Z^2 on lanes 0..3
+  const fq_t s1 = dq_xchg(sq, 1, mask), s2 = dq_xchg(sq, 2, mask), s3 = dq_xchg(sq, 3, mask);
+  // the square of lane j sits in sq, s1, s2 or s3 as j ^ l is 0, 1, 2 or 3
+  const fq_t A = pick4(l, sq, s1, s2, s3), S = pick4(l, s1, sq, s3, s2);
+  const fq_t B = pick4(l, s2, s3, sq, s1), ZZ = pick4(l, s3, s2, s1, sq);
   const fq_t C = fq_dbl(ZZ);
-  const fq_t D = fq_neg(A);
   const fq_t E = fq_sub(fq_sub(S, A), B);
-  const fq_t G = fq_add(D, B);
+  const fq_t G = fq_sub(B, A);
   const fq_t F = fq_sub(G, C);
-  const fq_t H = fq_sub(D, B);
-  const fq_t pr = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
-  xyzt_t r;
-  r.x = shfl4(pr, 0, mask);
-  r.y = shfl4(pr, 1, mask);
-  r.t = shfl4(pr, 2, mask);
-  r.z = shfl4(pr, 3, mask);
-  return r;
+  const fq_t H = fq_sub(fq_neg(A), B);
+  return fq_mul(pick4(l, E, E, G, F), pick4(l, F, H, H, G));
 }
 
-__device__ __noinline__ xyzt_t te_add_quad(const xyzt_t &p, const xyzt_t &q, uint32_t mask) {
+// add-2008-hwcd-3 with k = 2d (the same formula as te_add)
+static __device__ __noinline__ fq_t dq_add(fq_t p, fq_t q, uint32_t mask) {
   const uint32_t kc[FQ_LIMBS] = BLS_TE_K;
-  const int l = threadIdx.x & 3;
-  const fq_t m1 = pick4(l, fq_sub(p.y, p.x), fq_add(p.y, p.x), p.t, p.z);
-  const fq_t m2 = pick4(l, fq_sub(q.y, q.x), fq_add(q.y, q.x), q.t, q.z);
-  const fq_t pr = fq_mul(m1, m2);
-  const fq_t A = shfl4(pr, 0, mask), B = shfl4(pr, 1, mask), TT = shfl4(pr, 2, mask), ZZ = shfl4(pr, 3, mask);
-  const fq_t C = fq_mul(TT, fq_from(kc));
-  const fq_t D = fq_dbl(ZZ);
-  const fq_t E = fq_sub(B, A);
-  const fq_t F = fq_sub(D, C);
-  const fq_t G = fq_add(D, C);
-  const fq_t H = fq_add(B, A);
-  const fq_t pr2 = fq_mul(pick4(l, E, G, E, F), pick4(l, F, H, H, G));
-  xyzt_t r;
-  r.x = shfl4(pr2, 0, mask);
-  r.y = shfl4(pr2, 1, mask);
-  r.t = shfl4(pr2, 2, mask);
-  r.z = shfl4(pr2, 3, mask);
-  return r;
+  const int l = dq_lane();
+  const fq_t po = dq_xchg(p, 2, mask), qo = dq_xchg(q, 2, mask);  // lanes 0, 2 swap X and Y
+  // lane 0: (Y1 - X1)(Y2 - X2) = A, lane 2: (Y1 + X1)(Y2 + X2) = B, lane 1: T1 T2, lane 3: Z1 Z2
+  const fq_t m1 = l == 0 ? fq_sub(po, p) : l == 2 ? fq_add(p, po) : p;
+  const fq_t m2 = l == 0 ? fq_sub(qo, q) : l == 2 ? fq_add(q, qo) : q;
+  fq_t pr = fq_mul(m1, m2);
+  const fq_t kpr = fq_mul(pr, fq_from(kc));
+  pr = l == 1 ? kpr : l == 3 ? fq_dbl(pr) : pr;  // lane 1: C = k T1 T2, lane 3: D = 2 Z1 Z2
+  // pairs {0, 2} (A, B) and {1, 3} (C, D): E = B - A, H = B + A on lanes 0, 2; F = D - C,
+  // G = D + C on lanes 1, 3
+  const fq_t o = dq_xchg(pr, 2, mask);
+  const fq_t lo = l < 2 ? pr : o, hi = l < 2 ? o : pr;
+  const fq_t u = fq_sub(hi, lo), w = fq_add(hi, lo);
+  const fq_t u1 = dq_xchg(u, 1, mask);  // lane 0 gets F, lane 1 gets E
+  const fq_t w3 = dq_xchg(w, 3, mask);  // lane 1 gets H, lane 2 gets G
+  // X3 = E F (lane 0), T3 = E H (lane 1), Y3 = G H (lane 2), Z3 = F G (lane 3)
+  return fq_mul(pick4(l, u, u1, w3, u), pick4(l, u1, w3, w, w));
 }
 
 constexpr int kRedThreads = 256;
@@ -703,11 +724,10 @@ constexpr uint32_t kAllLanes = 0xffffffffu;
 // each tree level the 3 x stride additions are spread over the quads, so the three trees take 7
 // rounds of dependent additions instead of 18.  Only warps holding an active quad add (whole
 // warps, so their shuffles stay converged).  The sums are valid in quad 0.
-__device__ __forceinline__ void block_sum3(xyzt_t (&X)[3], uint4 *sh) {
-  const uint32_t q = threadIdx.x >> 2, ql = threadIdx.x & 3;
+__device__ __forceinline__ void block_sum3(fq_t (&X)[3], uint4 *sh) {
+  const uint32_t q = threadIdx.x >> 2;
   const uint32_t warp_q0 = (threadIdx.x >> 5) * 8;  // first quad of this warp
-  if (ql == 0)
-    for (int k = 0; k < 3; k++) xyzt_store(sh + (k * kRedQuads + q) * 12, X[k]);
+  for (int k = 0; k < 3; k++) dq_store(sh + (k * kRedQuads + q) * 12, X[k]);
   __syncthreads();
 #pragma unroll 1
   for (uint32_t stride = kRedQuads / 2; stride > 0; stride >>= 1) {
@@ -716,32 +736,32 @@ __device__ __forceinline__ void block_sum3(xyzt_t (&X)[3], uint4 *sh) {
       const uint32_t u = u0 + q;  // item u: array u / stride, element u % stride
       const bool act = u < 3 * stride;
       const uint32_t slot = act ? (u / stride) * kRedQuads + u % stride : 0;
-      xyzt_t a = xyzt_identity(), o = xyzt_identity();
+      fq_t a = dq_identity(), o = dq_identity();
       if (act) {
-        xyzt_load(a, sh + slot * 12);
-        xyzt_load(o, sh + (slot + stride) * 12);
+        a = dq_load(sh + slot * 12);
+        o = dq_load(sh + (slot + stride) * 12);
       }
-      if (u0 + warp_q0 < 3 * stride) a = te_add_quad(a, o, kAllLanes);
+      if (u0 + warp_q0 < 3 * stride) a = dq_add(a, o, kAllLanes);
       __syncthreads();
-      if (act && ql == 0) xyzt_store(sh + slot * 12, a);
+      if (act) dq_store(sh + slot * 12, a);
       __syncthreads();
     }
   }
-  for (int k = 0; k < 3; k++) xyzt_load(X[k], sh + k * kRedQuads * 12);
+  for (int k = 0; k < 3; k++) X[k] = dq_load(sh + k * kRedQuads * 12);
 }
 
 // Inclusive suffix sums over the quads: quad u gets sum_{v >= u} X_v (Hillis-Steele).
-__device__ __forceinline__ xyzt_t block_suffix_scan(xyzt_t X, uint4 *sh) {
-  const uint32_t q = threadIdx.x >> 2, ql = threadIdx.x & 3;
-  if (ql == 0) xyzt_store(sh + q * 12, X);
+__device__ __forceinline__ fq_t block_suffix_scan(fq_t X, uint4 *sh) {
+  const uint32_t q = threadIdx.x >> 2;
+  dq_store(sh + q * 12, X);
   __syncthreads();
 #pragma unroll 1
   for (uint32_t d = 1; d < kRedQuads; d <<= 1) {
-    xyzt_t o = xyzt_identity();
-    if (q + d < kRedQuads) xyzt_load(o, sh + (q + d) * 12);
+    fq_t o = dq_identity();
+    if (q + d < kRedQuads) o = dq_load(sh + (q + d) * 12);
     __syncthreads();
-    X = te_add_quad(X, o, kAllLanes);
-    if (ql == 0) xyzt_store(sh + q * 12, X);
+    X = dq_add(X, o, kAllLanes);
+    dq_store(sh + q * 12, X);
     __syncthreads();
   }
   return X;
@@ -754,7 +774,7 @@ __device__ __forceinline__ xyzt_t block_suffix_scan(xyzt_t X, uint4 *sh) {
 // where sum_u u RR_u = sum_{u >= 1} (suffix sum of RR at u): one block scan and three block
 // sums (run together), and only quad 0 doubles.
 __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log2, bool want_r,
-                              uint4 *sh, xyzt_t &A_out, xyzt_t &R_out) {
+                              uint4 *sh, fq_t &A_out, fq_t &R_out) {
   const uint32_t q = threadIdx.x >> 2;
   uint32_t per = 1, per_log2 = 0;
   while (per * kRedQuads < cnt) {
@@ -762,32 +782,31 @@ __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log
     per_log2++;
   }
   const uint32_t i0 = q * per;
-  xyzt_t SA = xyzt_identity(), T = xyzt_identity(), RR = xyzt_identity();
+  fq_t SA = dq_identity(), T = dq_identity(), RR = dq_identity();
 #pragma unroll 1
   for (uint32_t k = per; k-- > 0;) {  // runs past cnt are the identity
     const uint32_t i = i0 + k;
-    T = te_add_quad(T, RR, kAllLanes);
-    xyzt_t R = xyzt_identity(), A = xyzt_identity();
+    T = dq_add(T, RR, kAllLanes);
+    fq_t R = dq_identity(), A = dq_identity();
     if (i < cnt) {
-      xyzt_load(R, items + (size_t)i * 24);
-      xyzt_load(A, items + (size_t)i * 24 + 12);
+      R = dq_load(items + (size_t)i * 24);
+      A = dq_load(items + (size_t)i * 24 + 12);
     }
-    RR = te_add_quad(RR, R, kAllLanes);
-    SA = te_add_quad(SA, A, kAllLanes);
+    RR = dq_add(RR, R, kAllLanes);
+    SA = dq_add(SA, A, kAllLanes);
   }
-  const xyzt_t suf = block_suffix_scan(RR, sh);
+  const fq_t suf = block_suffix_scan(RR, sh);
   if (want_r && q == 0) R_out = suf;  // suffix at 0 is the total
-  xyzt_t S[3] = {q ? suf : xyzt_identity(), T, SA};
+  fq_t S[3] = {q ? suf : dq_identity(), T, SA};
   block_sum3(S, sh);
-  const xyzt_t &sumT = S[1], &sumSA = S[2];
   if (q == 0) {  // lanes 0..3 of warp 0
-    xyzt_t X = S[0];
+    fq_t X = S[0];
 #pragma unroll 1
-    for (uint32_t k = 0; k < per_log2; k++) X = te_dbl_quad(X, 0xfu);
-    X = te_add_quad(sumT, X, 0xfu);
+    for (uint32_t k = 0; k < per_log2; k++) X = dq_dbl(X, 0xfu);
+    X = dq_add(S[1], X, 0xfu);
 #pragma unroll 1
-    for (uint32_t k = 0; k < lin_log2; k++) X = te_dbl_quad(X, 0xfu);
-    A_out = te_add_quad(X, sumSA, 0xfu);
+    for (uint32_t k = 0; k < lin_log2; k++) X = dq_dbl(X, 0xfu);
+    A_out = dq_add(X, S[2], 0xfu);
   }
 }
 
@@ -800,12 +819,51 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce2(PassBuffers pb) {
   const uint32_t G = 1u << pb.grp_len_log2;
   const uint32_t first = (g - wd.grp_begin) * G;
   const uint32_t cnt = min(G, wd.nseg - first);
-  xyzt_t A, R;
+  fq_t A, R;
   block_combine(pb.seg_out + (size_t)(wd.seg_begin + first) * 24, cnt, pb.red_len_log2, true, sh, A, R);
-  if (threadIdx.x == 0) {
-    xyzt_store(pb.grp_out + (size_t)g * 24, R);
-    xyzt_store(pb.grp_out + (size_t)g * 24 + 12, A);
+  if (threadIdx.x < 4) {  // quad 0: one coordinate per lane
+    dq_store(pb.grp_out + (size_t)g * 24, R);
+    dq_store(pb.grp_out + (size_t)g * 24 + 12, A);
   }
+}
+
+// Windows of at most kRed3SmallMax groups (windowed MSMs: 2^(c-1) buckets make a few groups)
+// are combined by one quad each, in order:
+//   A = sum_i A_i + 2^lin sum_i i R_i,  sum_i i R_i = sum_{i >= 1} (suffix sum of R at i),
+// so hundreds of windows run side by side instead of one block each.  The quads of a warp work
+// on different windows, so each shuffles under its own 4-lane mask.
+constexpr uint32_t kRed3SmallMax = 16;
+
+__global__ void __launch_bounds__(128) k_reduce3_small(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;  // one window per quad
+  if (gw >= pb.n_wins) return;
+  const WinDesc wd = pb.wins[gw];
+  const uint32_t n = wd.ngrp;
+  if (n == 0 || n > kRed3SmallMax) return;
+  const uint32_t mask = 0xfu << (threadIdx.x & 28);
+  const uint32_t lin = pb.red_len_log2 + pb.grp_len_log2;
+  const uint4 *items = pb.grp_out + (size_t)wd.grp_begin * 24;
+  fq_t RR = dq_load(items + (size_t)(n - 1) * 24);
+  fq_t SA = dq_load(items + (size_t)(n - 1) * 24 + 12);
+  fq_t T = n >= 2 ? RR : dq_identity();
+#pragma unroll 1
+  for (uint32_t i = n - 1; i-- > 0;) {
+    const fq_t R = dq_load(items + (size_t)i * 24);
+    const fq_t A = dq_load(items + (size_t)i * 24 + 12);
+    SA = dq_add(SA, A, mask);
+    if (i >= 1) {
+      RR = dq_add(RR, R, mask);
+      T = dq_add(T, RR, mask);
+    }
+  }
+  fq_t out = SA;
+  if (n >= 2) {
+#pragma unroll 1
+    for (uint32_t k = 0; k < lin; k++) T = dq_dbl(T, mask);
+    out = dq_add(T, SA, mask);
+  }
+  dq_store(pb.win_sum + (size_t)gw * 12, out);
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
@@ -814,10 +872,46 @@ __global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
   if (gw >= pb.n_wins) return;
   __shared__ uint4 sh[3 * kRedQuads * 12];
   const WinDesc wd = pb.wins[gw];
-  xyzt_t A, R;
+  if (wd.ngrp <= kRed3SmallMax) return;  // k_reduce3_small's
+  fq_t A, R;
   block_combine(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp, pb.red_len_log2 + pb.grp_len_log2,
                 false, sh, A, R);
-  if (threadIdx.x == 0) xyzt_store(pb.win_sum + (size_t)gw * 12, A);
+  if (threadIdx.x < 4) dq_store(pb.win_sum + (size_t)gw * 12, A);
+}
+
+// Buckets split into more than kMergeWarpMax runs: a block of 64 quads per bucket, each quad
+// summing a strided share of the partials, then a tree over the quads in shared memory.
+__global__ void __launch_bounds__(kRedThreads) k_merge_big(PassBuffers pb) {
+  if (pb.counters[CNT_ERROR]) return;
+  __shared__ uint4 sh[kRedQuads * 12];
+  const uint32_t q = threadIdx.x >> 2;
+  const uint32_t warp_q0 = (threadIdx.x >> 5) * 8;  // first quad of this warp
+  const uint32_t nheavy = pb.counters[CNT_HEAVY];
+  for (uint32_t h = blockIdx.x; h < nheavy; h += gridDim.x) {
+    const uint32_t b = pb.heavy[h];
+    const uint32_t nt = ntask_of(pb.count[b], pb.seg_len);
+    if (nt <= kMergeWarpMax) continue;  // block-uniform
+    const uint32_t t0 = pb.taskoff[b];
+    fq_t acc = dq_identity();
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < nt; k0 += kRedQuads) {  // the same trip count for every quad
+      const fq_t p = k0 + q < nt ? dq_load(pb.partials + (size_t)(t0 + k0 + q) * 12) : dq_identity();
+      acc = dq_add(acc, p, kAllLanes);
+    }
+    dq_store(sh + q * 12, acc);
+    __syncthreads();
+#pragma unroll 1
+    for (uint32_t stride = kRedQuads / 2; stride > 0; stride >>= 1) {
+      fq_t o = dq_identity();
+      if (q < stride) o = dq_load(sh + (q + stride) * 12);
+      if (warp_q0 < stride) acc = dq_add(acc, o, kAllLanes);
+      __syncthreads();
+      if (q < stride) dq_store(sh + q * 12, acc);
+      __syncthreads();
+    }
+    if (threadIdx.x < 4) dq_store(pb.partials + (size_t)t0 * 12, acc);
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -853,18 +947,22 @@ __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
     return;
   }
   // Horner over the windows: acc = 2^c * acc + WS_w (pippenger.h:36-45 doubles per offset)
-  xyzt_t acc = xyzt_identity();
+  fq_t dacc = dq_identity();
   if (jd.n > 0 && jd.nred > 0) {
-    xyzt_load(acc, pb.win_sum + (size_t)(jd.win_begin + jd.nred - 1) * 12);
+    dacc = dq_load(pb.win_sum + (size_t)(jd.win_begin + jd.nred - 1) * 12);
 #pragma unroll 1
     for (int w = (int)jd.nred - 2; w >= 0; w--) {
 #pragma unroll 1
-      for (uint32_t k = 0; k < jd.c; k++) acc = te_dbl_quad(acc, 0xfu);
-      xyzt_t ws;
-      xyzt_load(ws, pb.win_sum + (size_t)(jd.win_begin + w) * 12);
-      acc = te_add_quad(acc, ws, 0xfu);
+      for (uint32_t k = 0; k < jd.c; k++) dacc = dq_dbl(dacc, 0xfu);
+      dacc = dq_add(dacc, dq_load(pb.win_sum + (size_t)(jd.win_begin + w) * 12), 0xfu);
     }
   }
+  // gather the point on lane 0 (lane 1 holds T, lane 2 Y, lane 3 Z)
+  xyzt_t acc;
+  acc.x = dacc;
+  acc.t = dq_xchg(dacc, 1, 0xfu);
+  acc.y = dq_xchg(dacc, 2, 0xfu);
+  acc.z = dq_xchg(dacc, 3, 0xfu);
   if (threadIdx.x != 0) return;
   wpt_t res = te_to_weierstrass(acc);  // z is 1, or 0 for infinity
   bool added = false;
@@ -995,6 +1093,8 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   launched++;
   k_merge<<<num_sms, 256, 0, st>>>(pb);
   launched++;
+  k_merge_big<<<num_sms * 3, kRedThreads, 0, st>>>(pb);
+  launched++;
   mark(6);
   if (pb.n_segs > 0) {
     k_reduce1<<<(pb.n_segs + 127) / 128, 128, 0, st>>>(pb);
@@ -1007,6 +1107,8 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
   }
   mark(8);
   if (pb.n_wins > 0) {
+    k_reduce3_small<<<(pb.n_wins + 31) / 32, 128, 0, st>>>(pb);
+    launched++;
     k_reduce3<<<pb.n_wins, kRedThreads, 0, st>>>(pb);
     launched++;
   }
