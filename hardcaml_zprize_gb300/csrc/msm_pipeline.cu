@@ -1,14 +1,18 @@
 // The MSM pipeline of one pass (one or many MSMs sharing one sort), all on the device:
 //
-//   1. k_count     signed c-bit digits of every scalar, histogram of (MSM, window, |digit|) keys
+//   1. k_count     signed c-bit digits of every scalar, histogram of (MSM, window, |digit|) keys;
+//                  stages each block's entries by key range (and uploads host scalars)
 //   2. k_scan_*    exclusive scans -> bucket offsets in the sorted array and task offsets
-//   3. k_scatter   counting-sort scatter of (base index | sign) into bucket order
+//   3. k_scatter_staged  counting-sort scatter of (base index | sign) into bucket order, one
+//                  launch per key range (k_scatter: the same from the scalars, for passes
+//                  without a stage)
 //   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
 //   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
 //   6. k_merge_*   buckets split over several runs: sum of their partials (a thread, a warp or
 //                  a block per bucket, by the number of runs)
 //   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33)
-//   8. k_reduce2/3 combine runs into groups, groups into window sums
+//   8. k_reduce2/3 combine runs into groups, groups into window sums (k_reduce3_small: one
+//                  quad per window of few groups)
 //   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
 //                  Weierstrass, add the bases without a twisted-Edwards image
 //                  (driver.cpp:349-372), write g1_projective_t (bls12_377_g1.h:427-439, 667-690)
