@@ -728,10 +728,15 @@ int init_device(Ctx *cx) {
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, cx->device));
   cx->num_sms = prop.multiProcessorCount;
-  int pageable = 0;
+  // kernels read pageable host memory through the host's page tables (address translation
+  // services over a coherent link, as on Grace); HMM systems report pageable access without
+  // host page tables and keep the copy path
+  int pageable = 0, host_tables = 0;
   CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, cx->device));
+  CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                            cx->device));
   const char *hp = getenv("MSM_HOST_PULL");
-  cx->host_pull = pageable != 0 && !(hp && strcmp(hp, "0") == 0);
+  cx->host_pull = pageable != 0 && host_tables != 0 && !(hp && strcmp(hp, "0") == 0);
   CK(cudaStreamCreateWithFlags(&cx->stream, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&cx->copy_stream, cudaStreamNonBlocking));
   for (int i = 0; i < 2; i++) {
