@@ -128,9 +128,19 @@ struct Cfg {
   uint32_t c = 16;
   uint32_t signed_digits = 1;
   uint32_t seg_len = 1024;
-  uint32_t red_log2 = 4;
+  uint32_t red_log2 = 0;  // level-1 reduction run length (log2); 0: chosen from the pass's buckets
   uint32_t fixed = 0;  // use the context's fixed-base tables (c is then the tables' width)
 };
+
+// Level-1 reduction runs of 2^red buckets, 16 to 64: passes of more than 2^21 buckets take
+// longer runs (about 2^17 of them still keep k_reduce1 at the product throughput), which leaves
+// fewer groups for the latency-bound level 2.  Measured on GB300: 16 is best at 2^19 and 2^21
+// buckets, 32 at 4.8 M (the uneven 64-MSM mix), 64 at 2^23.
+uint32_t red_log2_for(uint64_t buckets) {
+  int lg = 0;
+  while (lg < 63 && (2ull << lg) <= buckets) lg++;  // floor(log2(buckets))
+  return (uint32_t)std::min(6, std::max(4, lg - 17));
+}
 
 constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
 
@@ -189,7 +199,7 @@ Cfg heuristic_cfg(uint64_t n) {
   uint32_t s = 32;
   while (s < 2 * mean && s < 4096) s <<= 1;
   cfg.seg_len = s;
-  cfg.red_log2 = 4;
+  cfg.red_log2 = 0;
   return cfg;
 }
 
@@ -227,6 +237,16 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   if (specs.empty()) return fail(ERR_ARG, "empty pass");
   pl.seg_len = specs[0].cfg.seg_len;
   pl.red_log2 = specs[0].cfg.red_log2;
+  if (pl.red_log2 == 0) {  // automatic: from the pass's bucket count
+    uint64_t total = 0;
+    for (const JobSpec &s : specs) {
+      if (s.n == 0) continue;
+      uint32_t nwin, nb, nbt;
+      layout(s.cfg.c, s.cfg.signed_digits, nwin, nb, nbt);
+      total += s.cfg.fixed ? std::max(nb, nbt) : (uint64_t)(nwin - 1) * nb + nbt;
+    }
+    pl.red_log2 = red_log2_for(total);
+  }
   uint64_t buckets = 0, segs = 0, wins = 0, grps = 0;
   char tmp[160];
   for (size_t j = 0; j < specs.size(); j++) {
@@ -558,7 +578,7 @@ Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
       cfg.c = cx->fb_c;
       cfg.signed_digits = 1;
       cfg.seg_len = seg_len_for(n, std::max(nb, nbt), nwin);
-      cfg.red_log2 = 4;
+      cfg.red_log2 = 0;
     }
   }
   if (opt) {
@@ -1187,7 +1207,13 @@ int msm_get_config(void *context, uint64_t npoints, msm_options_t *out) {
   out->window_bits = (int32_t)c.c;
   out->signed_digits = c.signed_digits ? 1 : 2;
   out->seg_len = (int32_t)c.seg_len;
-  out->red_len_log2 = (int32_t)c.red_log2;
+  uint32_t red = c.red_log2;
+  if (red == 0) {  // what a pass of this one MSM would use
+    uint32_t nwin, nb, nbt;
+    layout(c.c, c.signed_digits, nwin, nb, nbt);
+    red = red_log2_for(c.fixed ? std::max(nb, nbt) : (uint64_t)(nwin - 1) * nb + nbt);
+  }
+  out->red_len_log2 = (int32_t)red;
   out->use_graph = 0;
   out->mode = 1;
   out->fixed_base = c.fixed ? 1 : 2;
