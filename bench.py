@@ -534,8 +534,7 @@ def main():
                     help="plain: the default single-MSM line; fixed_base_4x: 4 MSMs over one "
                          "resident base set (use with --log2n 26)")
     args = ap.parse_args()
-    if args.warmup < 3 and args.impl == "ours":
-        pass
+    args.warmup = max(args.warmup, 3)  # timed numbers always follow at least 3 warm-up steps
     rank, world, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
