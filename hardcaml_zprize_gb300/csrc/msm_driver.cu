@@ -542,9 +542,16 @@ int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
     stats_out[0] = cnt[CNT_TASKS];
     stats_out[1] = cnt[CNT_HEAVY];
   }
-  if (cnt[CNT_ERROR])
-    return fail(ERR_STATE, "device bounds check %u fired (info %u)", cnt[CNT_ERROR],
-                cnt[CNT_ERROR_INFO]);
+  if (cnt[CNT_ERROR]) {
+    // the codes msm_pipeline.cu's kernels record (they skip the access that would be out of bounds)
+    static const char *const what[] = {
+        "", "sorted entries exceed the plan", "tasks exceed the plan", "scatter position out of range",
+        "task slot out of range", "base index out of range", "stage chunk overflow",
+        "staged bucket key out of range"};
+    const uint32_t code = cnt[CNT_ERROR];
+    return fail(ERR_STATE, "device bounds check %u fired (%s; info %u)", code,
+                code < sizeof(what) / sizeof(what[0]) ? what[code] : "unknown", cnt[CNT_ERROR_INFO]);
+  }
   return 0;
 }
 
