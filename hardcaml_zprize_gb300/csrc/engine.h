@@ -109,7 +109,7 @@ struct PassBuffers {
 
   uint32_t *count;              // [n_buckets]
   uint32_t *offset;             // [n_buckets]
-  uint32_t *fill;               // [n_buckets]
+  uint32_t *fill;               // [n_buckets] slot cursors (the scan seeds them with offset)
   uint32_t *taskoff;            // [n_buckets]
   uint32_t *scan_tmp;           // block partials for the scans
   uint32_t *vals;               // [max_entries]
