@@ -409,6 +409,24 @@ def test_staged_sort_key_ranges(engine, ocpu, monkeypatch, ranges):
             ctx.close()
 
 
+@pytest.mark.parametrize("seg_len", [512, 128, 32, 8])
+def test_merge_tiers(engine, ocpu, seg_len):
+    """A bucket split into few, tens or hundreds of runs is merged by a thread, a warp or a block
+    of quads: 4096 equal scalars put 4096 entries in one bucket per window, i.e. 8, 32, 128 or
+    512 runs for these run lengths."""
+    nb = 1 << 12
+    pts = ocpu.gen_bases(515, nb)
+    sc = np.concatenate([np.repeat(engine.generate_scalars(516, 1), nb, axis=0)])
+    mixed = engine.generate_scalars(517, nb, kind=1)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        for s in (sc, mixed):
+            out = ctx.mult_uneven([nb], [0], s, seg_len=seg_len)
+            assert np.array_equal(out[0], ocpu.msm(pts, s)), seg_len
+    finally:
+        ctx.close()
+
+
 def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
     """The reference's second edge case holds a representable base of order 4, whose doubling
     chain reaches the order-two point (0, -1) and then the identity; the tables stay exact.  (A
