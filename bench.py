@@ -38,6 +38,21 @@ C_MADD = 4116   # 7 Montgomery products x 588 IMAD (12 x 32-bit limbs)
 C_ADD = 5292    # 9 products
 
 
+def hbm_view(achieved_bytes_per_s):
+    """Algorithmic HBM rate of k_accumulate (144 B base + 4 B entry per point and window) against
+    the measured copy bandwidth in MEASURED_PEAKS.json, or the 6.8 TB/s fallback."""
+    peak, src = 6800.0, "fallback 6.8 TB/s"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        pass
+    if not achieved_bytes_per_s:
+        return None
+    a = achieved_bytes_per_s / 1e9
+    return {"achieved": a, "peak": peak, "unit": "GB/s", "frac": a / peak, "peak_source": src}
+
+
 def imad_model(n: int, c: int) -> float:
     w = math.ceil(253 / c)
     return n * w * C_MADD + w * 2 ** (c - 1) * 2 * C_ADD + 253 * C_ADD + w * C_ADD
@@ -296,6 +311,8 @@ def run_ours(args, rank, world, local):
             "frac_vs_lo_hi_pairs": (achieved / peaks["mad_lo_hi"]) if achieved else None,
             "msm_achieved": algorithmic_imad(n) / msm_s / 1e12,
             "msm_frac": algorithmic_imad(n) / msm_s / peak_imad,
+            # the same kernel against the copy bandwidth: how far it is from being memory-bound
+            "hbm": hbm_view(n * w_used * 148 / t_acc if t_acc > 0 else None),
         },
         "stages_ms": stage_acc,
         # achieved HBM rates of the two input streams: k_accumulate reads a 144 B base (table
