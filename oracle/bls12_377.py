@@ -473,6 +473,15 @@ def encode_scalar(k: int) -> bytes:
     return struct.pack("<4Q", *limbs64(k, 4))
 
 
+def encode_projective(p) -> bytes:
+    """An affine result as the engine writes it (bls12_377_g1.h:667-690): g1_projective_t with
+    Z = 1 in Montgomery form, (x R, y R, R); infinity as arkworks' zero(), (R, R, 0)."""
+    if p is INF:
+        return struct.pack("<18Q", *limbs64(to_mont(1), 6), *limbs64(to_mont(1), 6), *limbs64(0, 6))
+    return struct.pack("<18Q", *limbs64(to_mont(p[0]), 6), *limbs64(to_mont(p[1]), 6),
+                       *limbs64(to_mont(1), 6))
+
+
 def decode_projective(b: bytes):
     """g1_projective_t {x[6], y[6], z[6]} as an arkworks Jacobian point in Montgomery form ->
     canonical affine (what into_affine() returns)."""
