@@ -132,14 +132,14 @@ struct Cfg {
   uint32_t fixed = 0;  // use the context's fixed-base tables (c is then the tables' width)
 };
 
-// Level-1 reduction runs of 2^red buckets, 16 to 64: passes of more than 2^21 buckets take
+// Level-1 reduction runs of 2^red buckets, 8 to 64: passes of more than 2^21 buckets take
 // longer runs (about 2^17 of them still keep k_reduce1 at the product throughput), which leaves
-// fewer groups for the latency-bound level 2.  Measured on GB300: 16 is best at 2^19 and 2^21
-// buckets, 32 at 4.8 M (the uneven 64-MSM mix), 64 at 2^23.
+// fewer groups for the latency-bound level 2.  Measured on GB300: 8 is best at 2^15 buckets,
+// 16 at 2^21 (8 and 16 tie at 2^19), 32 at 4.8 M (the uneven 64-MSM mix), 64 at 2^23.
 uint32_t red_log2_for(uint64_t buckets) {
   int lg = 0;
   while (lg < 63 && (2ull << lg) <= buckets) lg++;  // floor(log2(buckets))
-  return (uint32_t)std::min(6, std::max(4, lg - 17));
+  return (uint32_t)std::min(6, std::max(lg <= 18 ? 3 : 4, lg - 17));
 }
 
 constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
@@ -183,6 +183,20 @@ double model_cost_fixed(uint64_t n, uint32_t c, uint32_t sgn) {
   return (double)n * nwin * 7.0 + (double)std::max(nb, nbt) * 24.0;
 }
 
+// Longest run of entries one accumulate thread sums: twice the mean bucket load (buckets of
+// `nwin_sharing` windows), so most buckets stay whole, but short enough that the n x nwin
+// entries make at least ~2^17 runs: with few, heavily loaded buckets (a fixed-base table of
+// small width) whole-bucket runs would leave most of the GPU idle.
+uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing, uint32_t nwin) {
+  const double mean = (double)n * nwin_sharing / std::max<uint32_t>(nb, 1);
+  uint32_t s = 32;
+  while (s < 2 * mean && s < 4096) s <<= 1;
+  const uint64_t entries = n * (uint64_t)nwin;
+  uint32_t cap = 16;
+  while (cap < 4096 && ((uint64_t)cap << 18) <= entries) cap <<= 1;  // entries / cap >= 2^17
+  return std::min(s, cap);
+}
+
 Cfg heuristic_cfg(uint64_t n) {
   Cfg cfg;
   double best = 1e300;
@@ -195,19 +209,9 @@ Cfg heuristic_cfg(uint64_t n) {
   }
   uint32_t nwin, nb, nbt;
   layout(cfg.c, 1, nwin, nb, nbt);
-  const double mean = (double)n / nb;  // entries per bucket per window
-  uint32_t s = 32;
-  while (s < 2 * mean && s < 4096) s <<= 1;
-  cfg.seg_len = s;
+  cfg.seg_len = seg_len_for(n, nb, 1, nwin);
   cfg.red_log2 = 0;
   return cfg;
-}
-
-uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing) {
-  const double mean = (double)n * nwin_sharing / std::max<uint32_t>(nb, 1);
-  uint32_t s = 32;
-  while (s < 2 * mean && s < 4096) s <<= 1;
-  return s;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -558,33 +562,42 @@ int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
 Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
   Cfg cfg = heuristic_cfg(n);
   auto it = cx->tuned.find(log2_ceil(std::max<uint64_t>(n, 1)));
-  if (it != cx->tuned.end()) cfg = it->second;
+  const bool tuned = it != cx->tuned.end();
+  if (tuned) cfg = it->second;
   const bool forced_c = opt && opt->window_bits > 0;
   if (opt) {
     if (forced_c) {
       cfg.c = (uint32_t)std::min(std::max(opt->window_bits, 4), 22);
       uint32_t nwin, nb, nbt;
       layout(cfg.c, 1, nwin, nb, nbt);
-      cfg.seg_len = seg_len_for(n, nb, 1);
+      cfg.seg_len = seg_len_for(n, nb, 1, nwin);
     }
     if (opt->signed_digits == 1) cfg.signed_digits = 1;
     if (opt->signed_digits == 2) cfg.signed_digits = 0;
   }
   if (!cfg.signed_digits && cfg.c > 21) cfg.c = 21;
+  const bool tuned_fixed = tuned && cfg.fixed && cx->fb_c;
   cfg.fixed = 0;
   // fixed-base tables: every window shares one bucket array and there is no serial window
-  // combine; chosen when the cost model says so (or when asked)
+  // combine; chosen when asked, by the tuner's measurement for this size class, or else when
+  // the cost model says so
   const int fb = opt ? opt->fixed_base : 0;
-  if (cx->fb_c && fb != 2 && (fb == 1 || !forced_c)) {
-    const double cf = model_cost_fixed(n, cx->fb_c, 1);
-    const double cs = model_cost(n, cfg.c, cfg.signed_digits);
-    if (fb == 1 || cf < cs) {
-      uint32_t nwin, nb, nbt;
-      layout(cx->fb_c, 1, nwin, nb, nbt);
-      cfg.fixed = 1;
-      cfg.c = cx->fb_c;
-      cfg.signed_digits = 1;
-      cfg.seg_len = seg_len_for(n, std::max(nb, nbt), nwin);
+  bool use_fixed = false;
+  if (cx->fb_c && fb != 2) {
+    if (fb == 1)
+      use_fixed = true;
+    else if (!forced_c)
+      use_fixed = tuned ? tuned_fixed
+                        : model_cost_fixed(n, cx->fb_c, 1) < model_cost(n, cfg.c, cfg.signed_digits);
+  }
+  if (use_fixed) {
+    uint32_t nwin, nb, nbt;
+    layout(cx->fb_c, 1, nwin, nb, nbt);
+    cfg.fixed = 1;
+    cfg.c = cx->fb_c;
+    cfg.signed_digits = 1;
+    if (!tuned_fixed) {
+      cfg.seg_len = seg_len_for(n, std::max(nb, nbt), nwin, nwin);
       cfg.red_log2 = 0;
     }
   }
@@ -728,21 +741,25 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
 // init: resident bases
 // ---------------------------------------------------------------------------------------------
 // Tuned configurations persisted by msm_tune (one line per size class:
-// "log2n c signed seg_len red_log2 ms"); the last line for a size class wins.
+// "log2n c signed seg_len red_log2 ms fixed"); the last line for a size class wins.
 void load_tune_cache(Ctx *cx) {
   const char *path = getenv("MSM_TUNE_CACHE");
   if (!path) return;
   FILE *f = fopen(path, "r");
   if (!f) return;
-  unsigned lg, c, sg, seg, red;
+  unsigned lg, c, sg, seg, red, fx;
   double ms;
-  while (fscanf(f, "%u %u %u %u %u %lf", &lg, &c, &sg, &seg, &red, &ms) == 6) {
-    if (lg > 40 || c < 4 || c > 22 || seg == 0 || seg > 4096 || red > 12) continue;
+  char line[256];
+  while (fgets(line, sizeof(line), f)) {
+    fx = 0;  // a seventh field (1: the fixed-base form) is optional
+    if (sscanf(line, "%u %u %u %u %u %lf %u", &lg, &c, &sg, &seg, &red, &ms, &fx) < 6) continue;
+    if (lg > 40 || c < 4 || c > 24 || seg == 0 || seg > 4096 || red > 12) continue;
     Cfg cf;
     cf.c = c;
     cf.signed_digits = sg ? 1 : 0;
     cf.seg_len = seg;
     cf.red_log2 = red;
+    cf.fixed = fx ? 1 : 0;
     cx->tuned[lg] = cf;
   }
   fclose(f);
@@ -798,7 +815,10 @@ uint32_t choose_fixed_base(uint64_t n) {
       return (uint32_t)c;
     if (strcmp(e, "auto")) return 0;
   }
-  if (n < (1ull << 20)) return 0;
+  // below 2^20 bases MSMs are latency-bound: the windowed form's serial combine (c (W - 1)
+  // dependent doublings, ~1.2 ms) dominates, and tables of width 16 (16 windows, 2^15 shared
+  // buckets, at most 2.4 GB) measured fastest or within 5% at 2^12..2^18 bases
+  if (n < (1ull << 20)) return fits(16) ? 16u : 0u;
   uint32_t best = 0;
   double best_cost = 1e300;
   for (uint32_t c = 11; c <= 24; c++) {
@@ -1277,6 +1297,15 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
       }
     }
   }
+  if (cx->fb_c) {  // the context's fixed-base tables, at the heuristic and a shorter run length
+    msm_options_t o{};
+    o.fixed_base = 1;
+    Cfg cf = resolve_cfg(cx, npoints, &o);
+    cands.push_back(cf);
+    Cfg cf2 = cf;
+    cf2.seg_len = std::max<uint32_t>(16, cf.seg_len / 4);
+    cands.push_back(cf2);
+  }
   std::lock_guard<std::mutex> lk(cx->mu);
   if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
   DevBuf dsc;
@@ -1291,6 +1320,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
   for (const Cfg &cf : cands) {
     std::vector<JobSpec> one(1);
     one[0] = {npoints, 0, 0, cf};
+    one[0].fb_stride = cf.fixed ? cx->npoints : 0;
     Plan pl;
     if (build_plan(one, pl)) continue;
     double t = 1e300;
@@ -1316,8 +1346,8 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
   cx->tuned[log2_ceil(npoints)] = best;
   if (const char *path = getenv("MSM_TUNE_CACHE")) {
     if (FILE *f = fopen(path, "a")) {
-      fprintf(f, "%u %u %u %u %u %.4f\n", log2_ceil(npoints), best.c, best.signed_digits,
-              best.seg_len, best.red_log2, best_ms);
+      fprintf(f, "%u %u %u %u %u %.4f %u\n", log2_ceil(npoints), best.c, best.signed_digits,
+              best.seg_len, best.red_log2, best_ms, best.fixed);
       fclose(f);
     }
   }
@@ -1328,7 +1358,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
     best_out->red_len_log2 = (int32_t)best.red_log2;
     best_out->use_graph = 0;
     best_out->mode = 1;
-    best_out->fixed_base = 2;
+    best_out->fixed_base = best.fixed ? 1 : 2;
   }
   return 0;
 }

@@ -87,11 +87,14 @@ def test_generated_bases_match_oracle(engine, ocpu):
 
 
 # ---- MSM parity -------------------------------------------------------------------------------
+@pytest.mark.parametrize("form", ["auto", "windowed"])
 @pytest.mark.parametrize("n", [1, 2, 3, 17, 64, 1000])
-def test_msm_small(engine, ref, ocpu, n):
+def test_msm_small(engine, ref, ocpu, n, form):
+    """Small contexts get fixed-base tables of width 16 (the default form); the windowed form
+    with its serial window combine is forced with fixed_base=2."""
     pts = ocpu.gen_bases(7 + n, n)
     sc = engine.generate_scalars(11 + n, 2 * n)
-    out = msm_gpu(engine, pts, sc)
+    out = msm_gpu(engine, pts, sc) if form == "auto" else msm_gpu(engine, pts, sc, fixed_base=2)
     for b in range(2):
         want = ocpu.msm(pts, sc[b * n:(b + 1) * n])
         assert np.array_equal(out[b], want), f"batch {b}"
@@ -239,7 +242,8 @@ def test_uneven_batch_modes(engine, ocpu):
     try:
         first = np.concatenate([[0], np.cumsum(sizes)])
         want = [ocpu.msm(pts[o:o + s], sc[first[j]:first[j] + s]) for j, (s, o) in enumerate(zip(sizes, offs))]
-        for opts in (dict(mode=1), dict(mode=2), dict(mode=2, use_graph=1), dict(mode=2, use_graph=2)):
+        for opts in (dict(mode=1), dict(mode=2), dict(mode=2, use_graph=1), dict(mode=2, use_graph=2),
+                     dict(mode=1, fixed_base=2), dict(mode=2, fixed_base=2)):
             for rep in range(2):
                 out = ctx.mult_uneven(sizes, offs, sc, **opts)
                 for j in range(len(sizes)):
