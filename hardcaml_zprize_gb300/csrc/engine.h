@@ -35,6 +35,7 @@ struct JobDesc {
   uint32_t fixed;         // 1: fixed-base tables, every window shares one bucket array
   uint32_t nred;          // windows of the bucket reduction (1 for fixed-base jobs)
   uint64_t fb_stride;     // base-table index step from one window's table to the next
+  uint64_t tab_base;      // first record of the job's table set in the resident base array
 };
 
 // One (MSM, window) pair for the bucket reduction.

@@ -129,7 +129,8 @@ struct Cfg {
   uint32_t signed_digits = 1;
   uint32_t seg_len = 1024;
   uint32_t red_log2 = 0;  // level-1 reduction run length (log2); 0: chosen from the pass's buckets
-  uint32_t fixed = 0;  // use the context's fixed-base tables (c is then the tables' width)
+  uint32_t fixed = 0;  // 1: the context's main fixed-base tables, 2: its width-16 tables (c is
+                       // then the tables' width); 0: windowed over the plain bases
 };
 
 // Level-1 reduction runs of 2^red buckets, 8 to 64: passes of more than 2^21 buckets take
@@ -221,7 +222,11 @@ struct JobSpec {
   uint64_t n, base_off, scalar_off;
   Cfg cfg;
   uint64_t fb_stride = 0;  // fixed-base jobs: index step between the windows' tables
+  uint64_t tab_base = 0;   // first record of the job's table set
 };
+
+struct Ctx;
+void set_tables(const Ctx *cx, JobSpec &s);
 
 struct Plan {
   std::vector<JobDesc> jobs;
@@ -270,8 +275,9 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
       d.nb = d.nb_top = 0;
     } else {
       layout(d.c, d.signed_digits, d.nwin, d.nb, d.nb_top);
-      d.fixed = s.cfg.fixed;
+      d.fixed = s.cfg.fixed ? 1 : 0;
       d.fb_stride = s.fb_stride;
+      d.tab_base = s.tab_base;
       d.nred = d.fixed ? 1 : d.nwin;
       const uint32_t L = 1u << pl.red_log2;
       for (uint32_t w = 0; w < d.nred; w++) {
@@ -412,6 +418,9 @@ struct Ctx {
   int num_sms = 0;
   uint64_t npoints = 0;
   uint32_t fb_c = 0, fb_w = 1;  // fixed-base tables: window width and windows (fb_c 0: none)
+  // second table set of width 16 after the main one (fb2_c 0: none), for the context's small
+  // MSMs: records [npoints * fb_w, npoints * (fb_w + fb2_w))
+  uint32_t fb2_c = 0, fb2_w = 0;
   DevBuf bases, flags, special_idx, special_cls, class_pts;
   uint32_t n_special = 0, n_classes = 0;
   cudaStream_t stream = nullptr, copy_stream = nullptr;
@@ -439,6 +448,12 @@ struct Ctx {
   }
 };
 
+// Where a job's entries point: the plain bases (windowed), the main tables or the width-16 set.
+void set_tables(const Ctx *cx, JobSpec &s) {
+  s.fb_stride = s.cfg.fixed ? cx->npoints : 0;
+  s.tab_base = s.cfg.fixed == 2 ? cx->npoints * cx->fb_w : 0;
+}
+
 PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars) {
   PassBuffers pb{};
   pb.bases = cx->bases.as<uint4>();
@@ -448,7 +463,7 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.class_pts = cx->class_pts.as<uint4>();
   pb.n_special = cx->n_special;
   pb.n_classes = cx->n_classes;
-  pb.n_bases = cx->npoints * cx->fb_w;
+  pb.n_bases = cx->npoints * (cx->fb_w + cx->fb2_w);
   pb.scalars = (const uint4 *)d_scalars;
   pb.jobs = ws.jobs.as<JobDesc>();
   pb.wins = ws.wins.as<WinDesc>();
@@ -576,27 +591,39 @@ Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
     if (opt->signed_digits == 2) cfg.signed_digits = 0;
   }
   if (!cfg.signed_digits && cfg.c > 21) cfg.c = 21;
-  const bool tuned_fixed = tuned && cfg.fixed && cx->fb_c;
+  // the table sets that exist: 1 main (width fb_c), 2 the width-16 set (fb2_c)
+  auto table_c = [&](uint32_t which) { return which == 1 ? cx->fb_c : which == 2 ? cx->fb2_c : 0u; };
+  const uint32_t tuned_fixed = tuned && table_c(cfg.fixed) ? cfg.fixed : 0u;
   cfg.fixed = 0;
   // fixed-base tables: every window shares one bucket array and there is no serial window
-  // combine; chosen when asked, by the tuner's measurement for this size class, or else when
-  // the cost model says so
+  // combine; chosen when asked (the cheaper set by the cost model), by the tuner's measurement
+  // for this size class, or else when the cost model says so
   const int fb = opt ? opt->fixed_base : 0;
-  bool use_fixed = false;
-  if (cx->fb_c && fb != 2) {
+  uint32_t use = 0;
+  if ((cx->fb_c || cx->fb2_c) && fb != 2) {
+    double best = 1e300;
+    uint32_t cheapest = 0;
+    for (uint32_t which = 1; which <= 2; which++) {
+      if (!table_c(which)) continue;
+      const double v = model_cost_fixed(n, table_c(which), 1);
+      if (v < best) {
+        best = v;
+        cheapest = which;
+      }
+    }
     if (fb == 1)
-      use_fixed = true;
+      use = cheapest;
     else if (!forced_c)
-      use_fixed = tuned ? tuned_fixed
-                        : model_cost_fixed(n, cx->fb_c, 1) < model_cost(n, cfg.c, cfg.signed_digits);
+      use = tuned ? tuned_fixed
+                  : (best < model_cost(n, cfg.c, cfg.signed_digits) ? cheapest : 0u);
   }
-  if (use_fixed) {
+  if (use) {
     uint32_t nwin, nb, nbt;
-    layout(cx->fb_c, 1, nwin, nb, nbt);
-    cfg.fixed = 1;
-    cfg.c = cx->fb_c;
+    layout(table_c(use), 1, nwin, nb, nbt);
+    cfg.fixed = use;
+    cfg.c = table_c(use);
     cfg.signed_digits = 1;
-    if (!tuned_fixed) {
+    if (tuned_fixed != use) {
       cfg.seg_len = seg_len_for(n, std::max(nb, nbt), nwin, nwin);
       cfg.red_log2 = 0;
     }
@@ -649,7 +676,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
       specs[j] = {sizes[j], offs[j], first[j], resolve_cfg(cx, sizes[j], opt)};
       specs[j].cfg.seg_len = resolve_cfg(cx, maxn, opt).seg_len;
       specs[j].cfg.red_log2 = resolve_cfg(cx, maxn, opt).red_log2;
-      specs[j].fb_stride = specs[j].cfg.fixed ? cx->npoints : 0;
+      set_tables(cx, specs[j]);
     }
     Plan pl;
     if (build_plan(specs, pl)) return g_err;
@@ -681,7 +708,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     uint64_t maxn = 0;
     for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
     one[0] = {maxn, 0, 0, resolve_cfg(cx, maxn, opt)};
-    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
+    set_tables(cx, one[0]);
     if (build_plan(one, probe)) return g_err;
     if (ws.ensure(probe)) return g_err;
   }
@@ -693,7 +720,7 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
   for (size_t j = 0; j < m; j++) {
     std::vector<JobSpec> one(1);
     one[0] = {sizes[j], offs[j], d_scalars ? first[j] : 0, resolve_cfg(cx, sizes[j], opt)};
-    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
+    set_tables(cx, one[0]);
     Plan pl;
     if (build_plan(one, pl)) return g_err;
     const void *src = d_scalars, *pull = nullptr;
@@ -759,7 +786,7 @@ void load_tune_cache(Ctx *cx) {
     cf.signed_digits = sg ? 1 : 0;
     cf.seg_len = seg;
     cf.red_log2 = red;
-    cf.fixed = fx ? 1 : 0;
+    cf.fixed = fx <= 2 ? fx : 0;
     cx->tuned[lg] = cf;
   }
   fclose(f);
@@ -832,11 +859,31 @@ uint32_t choose_fixed_base(uint64_t n) {
   return best;
 }
 
+// A second table set of width 16 for contexts of 2^20 bases or more whose main tables are
+// wider: the context's small MSMs (slices of a few thousand to a few hundred thousand points)
+// then skip the windowed form's serial window combine too.  Built when the automatic choice
+// made the main set (MSM_FIXED_BASE unset or "auto") and both sets fit the table budget.
+uint32_t choose_small_tables(uint64_t n, uint32_t fb_c, uint32_t fb_w) {
+  const char *e = getenv("MSM_FIXED_BASE");
+  if (e && strcmp(e, "auto")) return 0;
+  if (!fb_c || fb_c == 16 || n < (1ull << 20)) return 0;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
+  double budget = 160.0 * (1ull << 30);
+  if (const char *g = getenv("MSM_FIXED_BASE_MAX_GB")) budget = atof(g) * (1ull << 30);
+  budget = std::min(budget, (double)free_b - 16.0 * (1ull << 30));
+  const double w = fb_w + windows_of(16);
+  if ((double)n * w * MSM_BASE_BYTES > budget || (double)n * w >= 2147483647.0) return 0;
+  return 16;
+}
+
 int load_bases(Ctx *cx, const g1_affine_t *points, uint64_t n) {
   cx->npoints = n;
   cx->fb_c = choose_fixed_base(n);
   cx->fb_w = cx->fb_c ? windows_of(cx->fb_c) : 1;
-  CK(cx->bases.ensure(std::max<uint64_t>(n, 1) * cx->fb_w * MSM_BASE_BYTES));
+  cx->fb2_c = choose_small_tables(n, cx->fb_c, cx->fb_w);
+  cx->fb2_w = cx->fb2_c ? windows_of(cx->fb2_c) : 0;
+  CK(cx->bases.ensure(std::max<uint64_t>(n, 1) * (cx->fb_w + cx->fb2_w) * MSM_BASE_BYTES));
   CK(cx->flags.ensure(std::max<uint64_t>(n, 1)));
   CK(cx->special_idx.ensure(std::max<uint64_t>(n, 1) * 4));
   DevBuf cnt, staging;
@@ -867,6 +914,27 @@ int load_bases(Ctx *cx, const g1_affine_t *points, uint64_t n) {
     if (nfail) {  // a base of 2-power order: keep the plain table only
       cx->fb_c = 0;
       cx->fb_w = 1;
+      cx->fb2_c = 0;
+      cx->fb2_w = 0;
+    }
+  }
+  if (cx->fb2_c) {  // the width-16 set: window 0 is the plain table again
+    uint4 *region = cx->bases.as<uint4>() + n * cx->fb_w * 9;
+    CK(cudaMemcpyAsync(region, cx->bases.p, n * MSM_BASE_BYTES, cudaMemcpyDeviceToDevice,
+                       cx->stream));
+    DevBuf fb_fail;
+    CK(fb_fail.ensure(4));
+    CK(cudaMemsetAsync(fb_fail.p, 0, 4, cx->stream));
+    const uint64_t fchunk = 1ull << 20;
+    for (uint64_t i0 = 0; i0 < n; i0 += fchunk)
+      CK(msm_launch_fixed_base(region, cx->flags.as<uint8_t>(), n, i0, std::min(fchunk, n - i0),
+                               cx->fb2_c, cx->fb2_w, fb_fail.as<uint32_t>(), cx->stream));
+    uint32_t nfail = 0;
+    CK(cudaMemcpyAsync(&nfail, fb_fail.p, 4, cudaMemcpyDeviceToHost, cx->stream));
+    CK(cudaStreamSynchronize(cx->stream));
+    if (nfail) {
+      cx->fb2_c = 0;
+      cx->fb2_w = 0;
     }
   }
   uint32_t nspecial = 0;
@@ -1023,7 +1091,7 @@ struct Server {
   uint64_t request_bytes(uint64_t n) {
     std::vector<JobSpec> one(1);
     one[0] = {n, 0, 0, resolve_cfg(cx, n, nullptr)};
-    one[0].fb_stride = one[0].cfg.fixed ? cx->npoints : 0;
+    set_tables(cx, one[0]);
     Plan pl;
     if (build_plan(one, pl)) return ~0ull;
     return plan_bytes(pl, true);
@@ -1087,7 +1155,7 @@ void Server::loop() {
           specs[j] = {batch[j]->n, batch[j]->base_off, first, resolve_cfg(cx, batch[j]->n, nullptr)};
           specs[j].cfg.seg_len = big.seg_len;
           specs[j].cfg.red_log2 = big.red_log2;
-          specs[j].fb_stride = specs[j].cfg.fixed ? cx->npoints : 0;
+          set_tables(cx, specs[j]);
           first += batch[j]->n;
         }
         Slot &sl = *free_slot;
@@ -1297,10 +1365,17 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
       }
     }
   }
-  if (cx->fb_c) {  // the context's fixed-base tables, at the heuristic and a shorter run length
-    msm_options_t o{};
-    o.fixed_base = 1;
-    Cfg cf = resolve_cfg(cx, npoints, &o);
+  for (uint32_t which = 1; which <= 2; which++) {  // each table set, at two run lengths
+    const uint32_t tc = which == 1 ? cx->fb_c : cx->fb2_c;
+    if (!tc) continue;
+    uint32_t nwin, nb, nbt;
+    layout(tc, 1, nwin, nb, nbt);
+    Cfg cf;
+    cf.fixed = which;
+    cf.c = tc;
+    cf.signed_digits = 1;
+    cf.seg_len = seg_len_for(npoints, std::max(nb, nbt), nwin, nwin);
+    cf.red_log2 = 0;
     cands.push_back(cf);
     Cfg cf2 = cf;
     cf2.seg_len = std::max<uint32_t>(16, cf.seg_len / 4);
@@ -1320,7 +1395,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
   for (const Cfg &cf : cands) {
     std::vector<JobSpec> one(1);
     one[0] = {npoints, 0, 0, cf};
-    one[0].fb_stride = cf.fixed ? cx->npoints : 0;
+    set_tables(cx, one[0]);
     Plan pl;
     if (build_plan(one, pl)) continue;
     double t = 1e300;
@@ -1347,7 +1422,7 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
   if (const char *path = getenv("MSM_TUNE_CACHE")) {
     if (FILE *f = fopen(path, "a")) {
       fprintf(f, "%u %u %u %u %u %.4f %u\n", log2_ceil(npoints), best.c, best.signed_digits,
-              best.seg_len, best.red_log2, best_ms, best.fixed);
+              best.seg_len, best.red_log2, best_ms, best.fixed);  // fixed: 0, 1 main, 2 width 16
       fclose(f);
     }
   }
@@ -1735,7 +1810,7 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
   pb.class_pts = cx->class_pts.as<uint4>();
   pb.n_special = cx->n_special;
   pb.n_classes = cx->n_classes;
-  pb.n_bases = cx->npoints * cx->fb_w;
+  pb.n_bases = cx->npoints * (cx->fb_w + cx->fb2_w);
   pb.scalars = (const uint4 *)d_scalars;
   pb.jobs = (const JobDesc *)(s + o_jobs);
   pb.wins = (const WinDesc *)(s + o_wins);

@@ -123,7 +123,7 @@ __device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDes
     const int32_t d = next_digit(s, jd, w, carry);
     if (d == 0) continue;
     const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
-    const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
+    const uint64_t tidx = jd.tab_base + (jd.fixed ? (uint64_t)w * jd.fb_stride : 0) + bidx;
     const uint32_t val = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
     const uint32_t pos = atomicAdd(&sh_cur[key >> pb.bin_shift], 1u);
     if (pos < pb.stage_cap) {
@@ -339,7 +339,7 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
           ok[k] = true;
           key[k] = bucket_key(jd, w, (uint32_t)abs(d));
           ok[k] = key[k] >= key_lo && key[k] < key_hi;
-          const uint64_t tidx = jd.fixed ? (uint64_t)w * jd.fb_stride + bidx : bidx;
+          const uint64_t tidx = jd.tab_base + (jd.fixed ? (uint64_t)w * jd.fb_stride : 0) + bidx;
           val[k] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
         }
       }

@@ -431,6 +431,32 @@ def test_merge_tiers(engine, ocpu, seg_len):
         ctx.close()
 
 
+def test_width16_tables_on_a_large_context(engine, ocpu):
+    """A context of 2^20 bases holds its main tables (width 20) and a second set of width 16;
+    small MSMs over slices take the width-16 set, full-size ones the main set, and every form
+    (including windowed) matches the oracle."""
+    n = 1 << 20
+    pts = engine.generate_bases(4711, n)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        assert ctx.config(4096)["window_bits"] == 16 and ctx.config(4096)["fixed_base"] == 1
+        assert ctx.config(n)["window_bits"] == 20 and ctx.config(n)["fixed_base"] == 1
+        sizes = [4096, 50000, 1000, 1]
+        offs = [0, 123457, n - 1000, n - 1]
+        sc = np.concatenate([engine.generate_scalars(4712 + j, s, kind=1, msm_index=j)
+                             for j, s in enumerate(sizes)])
+        first = np.concatenate([[0], np.cumsum(sizes)])
+        want = [ocpu.msm(pts[o:o + s], sc[first[j]:first[j] + s]) for j, (s, o) in enumerate(zip(sizes, offs))]
+        for opts in (dict(mode=1), dict(mode=2), dict(mode=2, use_graph=1), dict(fixed_base=2)):
+            out = ctx.mult_uneven(sizes, offs, sc, **opts)
+            for j in range(len(sizes)):
+                assert np.array_equal(out[j], want[j]), (opts, j)
+        full = engine.generate_scalars(4720, n)
+        assert np.array_equal(ctx.mult(full)[0], ocpu.msm(pts, full))
+    finally:
+        ctx.close()
+
+
 def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
     """The reference's second edge case holds a representable base of order 4, whose doubling
     chain reaches the order-two point (0, -1) and then the identity; the tables stay exact.  (A
