@@ -2,12 +2,15 @@
 //
 // It mirrors the reference host driver (zprize/msm_pippenger/host/driver/driver.cpp):
 //   msm_init  -> Driver::Driver + load_xclbin (driver.cpp:137-304): bases converted once to the
-//                precomputed twisted-Edwards form, here on the GPU, and kept resident in HBM;
-//                bases without a twisted-Edwards image are listed for the Weierstrass path
-//                (driver.cpp:158-171);
-//   msm_mult  -> run_asynchronous (driver.cpp:495-600): scalars of batch b+1 cross PCIe/C2C while
-//                batch b computes; everything after the scalars (sort, buckets, reduction,
-//                window combine, affine map) runs on the device and only 144 B per MSM return.
+//                precomputed twisted-Edwards form, here on the GPU, and kept resident in HBM,
+//                with fixed-base tables 2^(c w) P_i when HBM allows (a second set of width 16
+//                for large contexts); bases without a twisted-Edwards image are listed for the
+//                Weierstrass path (driver.cpp:158-171);
+//   msm_mult  -> run_asynchronous (driver.cpp:495-600): the first MSM's scalars are read from
+//                host memory by the histogram kernel itself (Grace: over NVLink-C2C) and those of
+//                batch b+1 are copied while batch b computes; everything after the scalars (sort,
+//                buckets, reduction, window combine, affine map) runs on the device and only
+//                144 B per MSM return.
 // Additions: uneven batches in one pass with one shared sort, CUDA-graph replay, an autotuner,
 // a continuous-batching server, per-stage timing and data generators for tests and benchmarks.
 #include <cuda_runtime.h>
