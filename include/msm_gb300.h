@@ -52,8 +52,10 @@ typedef struct {
  * ------------------------------------------------------------------------------------------- */
 
 /* Load the bases once and keep them resident on the GPU in precomputed twisted-Edwards form.
- * For 2^20 bases or more, when HBM allows, it also keeps fixed-base tables 2^(c w) P_i for every
- * window w (environment: MSM_FIXED_BASE=0 off, =<c> force width c; MSM_FIXED_BASE_MAX_GB).
+ * When HBM allows it also keeps fixed-base tables 2^(c w) P_i for every window w (width from a
+ * cost model for 2^20 bases or more, 16 below; large contexts add a second set of width 16 for
+ * their small MSMs). Environment: MSM_FIXED_BASE=0 off, =<c> force width c (one set);
+ * MSM_FIXED_BASE_MAX_GB caps the tables.
  * Replaces `extern "C" Driver *msm_init(const char *xclbin, ssize_t xclbin_len,
  * g1_affine_t *rust_points, ssize_t npoints)` (zprize/msm_pippenger/host/driver/driver.cpp:603-617).
  * `xclbin` names an FPGA bitstream in the reference; here it is accepted and ignored (it may be
