@@ -101,8 +101,11 @@ struct PassBuffers {
   // staged sort (or stage == null: the scatter re-reads the scalars once per key range).
   // k_count writes the entries of its 256 points, (key, base index | sign << 31), into the
   // block's chunk of `stage`, grouped by key range (key >> bin_shift); blk_off holds each
-  // chunk's n_bins + 1 range starts.  The scatter then reads one key range per launch.
+  // chunk's n_bins + 1 range starts.  The scatter then reads one key range per launch and
+  // places each entry at offset + rank (stage_rank set) or at a slot-cursor atomic (null).
   uint2 *stage;                 // [n_chunks * stage_cap]
+  uint32_t *stage_rank;         // or null: [n_chunks * stage_cap] each staged entry's rank in its
+                                // bucket, taken from the bucket count when the entry is staged
   uint32_t *blk_off;            // [n_chunks * (n_bins + 1)]
   uint32_t stage_cap;           // entries per chunk: 256 x the pass's largest window count
   uint32_t bin_shift;           // key range of a bucket key

@@ -241,6 +241,7 @@ struct Plan {
   // largest window count of the pass, and the key ranges of the scatter
   uint64_t n_chunks = 0;
   uint32_t stage_cap = 0, bin_shift = 0, n_bins = 0;
+  bool ranks = false;  // entries carry their rank in the bucket (no slot atomics in the scatter)
   std::string key;
 };
 
@@ -322,6 +323,10 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u);
   pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
   if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
+  // ranks from the histogram's atomics save the scatter's slot atomics; on GB300 that won for
+  // 2^27.6 and 2^26.7 entries (2^24 points, the uneven mix) and lost for 2^29.5 (2^26 points,
+  // whose 2^23 bucket counters made the returning atomics slow)
+  pl.ranks = pl.max_entries < (1ull << 29);
   snprintf(tmp, sizeof(tmp), "|r%u", pl.bin_shift);
   pl.key += tmp;
   pl.n_segs = (uint32_t)segs;
@@ -339,7 +344,7 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
   uint64_t b = 0;
   b += (uint64_t)pl.n_buckets * 4 * 5;                   // count, offset, fill, taskoff, heavy
   b += pl.max_entries * 4;                                // vals
-  b += pl.n_chunks * ((uint64_t)pl.stage_cap * 8 + (pl.n_bins + 1) * 4);  // stage, blk_off
+  b += pl.n_chunks * ((uint64_t)pl.stage_cap * (pl.ranks ? 12 : 8) + (pl.n_bins + 1) * 4);
   b += (uint64_t)pl.max_tasks * (sizeof(Task) + 4 + MSM_BUCKET_BYTES);
   b += (uint64_t)(pl.n_segs + pl.n_grps) * 2 * MSM_BUCKET_BYTES;
   b += (uint64_t)pl.wins.size() * MSM_BUCKET_BYTES;
@@ -353,7 +358,7 @@ uint64_t plan_bytes(const Plan &pl, bool with_scalars) {
 // ---------------------------------------------------------------------------------------------
 struct Workspace {
   DevBuf count, offset, fill, taskoff, scan_tmp, vals, tasks, partials, heavy, counters, seg_out,
-      grp_out, win_sum, results, jobs, wins, order, len_hist, stage, blk_off;
+      grp_out, win_sum, results, jobs, wins, order, len_hist, stage, stage_rank, blk_off;
   DevBuf scalars[2];
   HostPinned res_host;
   cudaEvent_t ev[MSM_NUM_STAGES + 1] = {};
@@ -379,6 +384,7 @@ struct Workspace {
     CK(scan_tmp.ensure(msm_scan_tmp_words(pl.n_buckets) * 4, &moved));
     CK(vals.ensure((size_t)pl.max_entries * 4, &moved));
     CK(stage.ensure((size_t)pl.n_chunks * pl.stage_cap * 8, &moved));
+    if (pl.ranks) CK(stage_rank.ensure((size_t)pl.n_chunks * pl.stage_cap * 4, &moved));
     CK(blk_off.ensure((size_t)pl.n_chunks * (pl.n_bins + 1) * 4, &moved));
     CK(tasks.ensure((size_t)pl.max_tasks * sizeof(Task), &moved));
     CK(partials.ensure((size_t)pl.max_tasks * MSM_BUCKET_BYTES, &moved));
@@ -406,7 +412,7 @@ struct Workspace {
     graphs.clear();
     count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
     scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
-    stage.release(); blk_off.release();
+    stage.release(); stage_rank.release(); blk_off.release();
     order.release(); len_hist.release(); grp_out.release();
     win_sum.release(); scalars[0].release(); scalars[1].release();
     generation++;
@@ -489,6 +495,7 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.vals = ws.vals.as<uint32_t>();
   pb.stage = pl.n_chunks ? ws.stage.as<uint2>() : nullptr;
   pb.blk_off = ws.blk_off.as<uint32_t>();
+  pb.stage_rank = pl.ranks && pb.stage ? ws.stage_rank.as<uint32_t>() : nullptr;
   pb.stage_cap = pl.stage_cap;
   pb.bin_shift = pl.bin_shift;
   pb.n_bins = pl.n_bins;

@@ -100,6 +100,8 @@ __device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDes
     const int32_t d = next_digit(s, jd, w, carry);
     if (d == 0) continue;
     const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    if (sh_bins) atomicAdd(&sh_bins[key >> pb.bin_shift], 1u);
+    if (pb.stage_rank) continue;  // the bucket counts come with the ranks in stage_digits
     // a warp whose active lanes all hit one bucket (e.g. equal scalars) adds once; otherwise
     // every lane adds on its own (distinct buckets for uniform scalars)
     const uint32_t active = __activemask();
@@ -110,14 +112,14 @@ __device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDes
     } else {
       atomicAdd(&pb.count[key], 1u);
     }
-    if (sh_bins) atomicAdd(&sh_bins[key >> pb.bin_shift], 1u);
   }
 }
 
 // Round 2 of the staged sort: the entries of one point into the block's chunk, at the cursors
 // of their key ranges.
 __device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s,
-                                             uint64_t bidx, uint32_t *sh_cur, uint2 *chunk) {
+                                             uint64_t bidx, uint32_t *sh_cur, uint2 *chunk,
+                                             uint32_t *ranks) {
   uint32_t carry = 0;
   for (uint32_t w = 0; w < jd.nwin; w++) {
     const int32_t d = next_digit(s, jd, w, carry);
@@ -125,9 +127,26 @@ __device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDes
     const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
     const uint64_t tidx = jd.tab_base + (jd.fixed ? (uint64_t)w * jd.fb_stride : 0) + bidx;
     const uint32_t val = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
+    uint32_t rank = 0;
+    if (ranks) {
+      // the bucket count's old value is the entry's rank in its bucket (one atomic per warp
+      // when its active lanes share the bucket)
+      const uint32_t active = __activemask();
+      const int leader = __ffs(active) - 1;
+      const int lane = threadIdx.x & 31;
+      const uint32_t k0 = __shfl_sync(active, key, leader);
+      if (__all_sync(active, key == k0)) {
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&pb.count[key], (uint32_t)__popc(active));
+        rank = __shfl_sync(active, base, leader) + __popc(active & ((1u << lane) - 1u));
+      } else {
+        rank = atomicAdd(&pb.count[key], 1u);
+      }
+    }
     const uint32_t pos = atomicAdd(&sh_cur[key >> pb.bin_shift], 1u);
     if (pos < pb.stage_cap) {
       chunk[pos] = make_uint2(key, val);
+      if (ranks) ranks[pos] = rank;
     } else {
       set_error(pb.counters, 6, pos);
     }
@@ -188,7 +207,9 @@ __global__ void __launch_bounds__(MSM_POINTS_PER_CHUNK) k_count(PassBuffers pb, 
     bo[pb.n_bins] = acc;
   }
   __syncthreads();
-  if (ok) stage_digits(pb, jd, s, bidx, sh_cur, pb.stage + chunk * pb.stage_cap);
+  if (ok)
+    stage_digits(pb, jd, s, bidx, sh_cur, pb.stage + chunk * pb.stage_cap,
+                 pb.stage_rank ? pb.stage_rank + chunk * pb.stage_cap : nullptr);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -381,11 +402,21 @@ __global__ void __launch_bounds__(256) k_scatter_staged(PassBuffers pb, uint32_t
   const uint32_t *bo = pb.blk_off + chunk * (pb.n_bins + 1);
   const uint32_t lo = bo[bin], hi = min(bo[bin + 1], pb.stage_cap);
   const uint2 *st = pb.stage + chunk * pb.stage_cap;
+  const uint32_t *rk = pb.stage_rank ? pb.stage_rank + chunk * pb.stage_cap : nullptr;
   const int lane = threadIdx.x & 31;
   for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
     const uint2 kv = st[e];
     if (kv.x >= pb.n_buckets) {  // cannot happen for a consistent stage; never write out of bounds
       set_error(pb.counters, 7, kv.x);
+      continue;
+    }
+    if (rk) {  // position known from the rank: no atomic
+      const uint32_t p = pb.offset[kv.x] + rk[e];
+      if (p < pb.max_entries) {
+        pb.vals[p] = kv.y;
+      } else {
+        set_error(pb.counters, 3, p);
+      }
       continue;
     }
     uint32_t pos;
