@@ -271,15 +271,16 @@ def run_ours(args, rank, world, local):
     ms_per_step = 1e3 * t_dev / args.steps
     msm_s = t_dev / args.steps
     t_acc = stage_acc.get("accumulate", 0) * 1e-3
-    w_used = math.ceil(253 / cfg["window_bits"])
-    acc_imad = n * w_used * C_MADD
+    entries = int(stats["entries"])  # mixed adds of one pass: its nonzero digits
+    w_tab = 253 // cfg["window_bits"] + 1  # signed windows: fixed-base tables per base
+    acc_imad = entries * C_MADD
     achieved = acc_imad / t_acc if t_acc > 0 else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "k_accumulate_traffic.json")
     if os.path.exists(tf):
         try:
             tr = json.load(open(tf))
-            traffic = tr["bytes_per_point_window"] * n * w_used
+            traffic = tr["bytes_per_point_window"] * entries
         except Exception:
             traffic = None
     line = {
@@ -290,7 +291,7 @@ def run_ours(args, rank, world, local):
         "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n,
                    "l2": f"inputs larger than L2 ({n * 32 / 2**20:.0f} MB scalars, "
                          f"{n * 144 / 2**30:.2f} GB bases"
-                         + (f", {n * w_used * 144 / 2**30:.1f} GB fixed-base tables)" if cfg["fixed_base"] == 1 else ")"),
+                         + (f", {n * w_tab * 144 / 2**30:.1f} GB fixed-base tables)" if cfg["fixed_base"] == 1 else ")"),
                    "window_bits": cfg["window_bits"], "signed_digits": cfg["signed_digits"] == 1,
                    "seg_len": cfg["seg_len"], "red_len_log2": cfg["red_len_log2"],
                    "fixed_base_tables": cfg["fixed_base"] == 1},
@@ -304,7 +305,7 @@ def run_ours(args, rank, world, local):
             "achieved": achieved / 1e12 if achieved else None, "peak": peak_imad / 1e12,
             "unit": "TIMAD/s", "frac": (achieved / peak_imad) if achieved else None,
             "traffic": traffic,
-            "algorithmic_imad_per_launch": acc_imad,
+            "algorithmic_imad_per_launch": acc_imad, "entries_per_launch": entries,
             "peak_source": "measured in this run: independent mad.lo chains on all SMs "
                            "(msm_measure_int_peaks); algorithmic count 588 IMAD per 12-limb product",
             "peak_mad_lo_hi_pairs": peaks["mad_lo_hi"] / 1e12, "peak_mad_hi": peaks["mad_hi"] / 1e12,
@@ -312,13 +313,13 @@ def run_ours(args, rank, world, local):
             "msm_achieved": algorithmic_imad(n) / msm_s / 1e12,
             "msm_frac": algorithmic_imad(n) / msm_s / peak_imad,
             # the same kernel against the copy bandwidth: how far it is from being memory-bound
-            "hbm": hbm_view(n * w_used * 148 / t_acc if t_acc > 0 else None),
+            "hbm": hbm_view(entries * 148 / t_acc if t_acc > 0 else None),
         },
         "stages_ms": stage_acc,
         # achieved HBM rates of the two input streams: k_accumulate reads a 144 B base (table
         # entry) and a 4 B sorted entry per point and window; k_count reads the 32 B scalars
         "streams_gbs": {
-            "bases_in_accumulate": n * w_used * 148 / t_acc / 1e9 if t_acc > 0 else None,
+            "bases_in_accumulate": entries * 148 / t_acc / 1e9 if t_acc > 0 else None,
             "scalars_in_count": n * 32 / (stage_acc.get("count", 0) * 1e-3) / 1e9
             if stage_acc.get("count", 0) > 0 else None,
         },
@@ -406,6 +407,7 @@ def run_fixed_base_large(args, rank, world, local):
     ctx.set_timing(True)
     ctx.mult(sc[:n])
     stages = ctx.last_timings()
+    entries = int(ctx.last_pass_stats()["entries"])  # mixed adds of one MSM's pass
     ctx.set_timing(False)
     # parity by properties
     windowed = ctx.mult(sc[:n], fixed_base=2)[0]
@@ -414,7 +416,6 @@ def run_fixed_base_large(args, rank, world, local):
     lin = ref.add(ref.decode_projective(out[0].tobytes()), ref.decode_projective(out[1].tobytes())) == \
         ref.decode_projective(out2.tobytes())
     ctx.close()
-    w_used = math.ceil(253 / cfg["window_bits"])
     t_acc = stages.get("accumulate", 0) * 1e-3
     value = batches / t_all
     line = {
@@ -427,10 +428,11 @@ def run_fixed_base_large(args, rank, world, local):
         "e2e": {"value": value, "unit": "MSM/s", "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": 144},
         "per_batch_latency_ms": 1e3 * t_all / batches,
         "stages_ms": stages,
-        "hbm_gbs_base_and_scalar_streams": (n * w_used * 148 + n * 32) / t_acc / 1e9 if t_acc else None,
-        "imad": {"achieved_tera": n * w_used * C_MADD / t_acc / 1e12 if t_acc else None,
+        "hbm_gbs_base_and_scalar_streams": (entries * 148 + n * 32) / t_acc / 1e9 if t_acc else None,
+        "imad": {"achieved_tera": entries * C_MADD / t_acc / 1e12 if t_acc else None,
                  "peak_mad_lo_tera": peaks["mad_lo"] / 1e12,
-                 "frac": (n * w_used * C_MADD / t_acc / peaks["mad_lo"]) if t_acc else None},
+                 "frac": (entries * C_MADD / t_acc / peaks["mad_lo"]) if t_acc else None,
+                 "entries_per_msm": entries},
         "parity": {"fixed_base_equals_windowed": bool(np.array_equal(out[0], windowed)),
                    "linearity": bool(lin)},
         "setup_s": {"generate_bases": t_gen, "msm_init_with_tables": t_init},

@@ -226,7 +226,7 @@ class MultiScalarMultContext:
     def last_pass_stats(self) -> dict:
         arr = (ctypes.c_uint64 * 5)()
         load_library().msm_last_pass_stats(self.handle, arr, 5)
-        return {"tasks": arr[0], "heavy_buckets": arr[1], "max_entries": arr[2], "buckets": arr[3],
+        return {"tasks": arr[0], "heavy_buckets": arr[1], "entries": arr[2], "buckets": arr[3],
                 "kernels": arr[4]}
 
     def mult_noalloc(self, n: int, base_offset: int, d_scalars_ptr: int, d_out_ptr: int,

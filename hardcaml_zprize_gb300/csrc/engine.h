@@ -64,6 +64,7 @@ enum : int {
   CNT_HEAVY_CURSOR = 3,
   CNT_ERROR = 4,          // nonzero: a device-side bounds check fired (code)
   CNT_ERROR_INFO = 5,
+  CNT_ENTRIES = 6,        // sorted entries of the pass (nonzero digits)
   CNT_WORDS = 8,
 };
 

@@ -148,6 +148,10 @@ uint32_t red_log2_for(uint64_t buckets) {
 
 constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
 
+// the scalar field's modulus r, little-endian 64-bit words
+const uint64_t R_WORDS[4] = {0x0a11800000000001ull, 0x59aa76fed0000001ull, 0x60b44d1e5c37b001ull,
+                             0x12ab655e9a2ca556ull};
+
 uint32_t windows_of(uint32_t c) { return (MSM_SCALAR_BITS + c - 1) / c; }
 
 uint32_t log2_ceil(uint64_t n) {
@@ -156,18 +160,32 @@ uint32_t log2_ceil(uint64_t n) {
   return k;
 }
 
-// bucket counts of a window layout (signed: 2^(c-1) per window, the top one 2^c_top; unsigned:
-// 2^c - 1 and 2^c_top - 1)
+// Bucket counts of a window layout: signed 2^(c-1) per window, unsigned 2^c - 1.  The top window
+// holds the c_top = 253 - c (W-1) bits left over: unsigned 2^c_top - 1 buckets; signed (its
+// digit also takes the carry out of the window below) 2^c_top, capped at the largest top digit a
+// scalar below r produces, floor((r-1) / 2^(c (W-1))) + 1.  A 253-bit scalar at or above r whose
+// top digit is larger gets it as two entries (see entries_per_point).
 void layout(uint32_t c, uint32_t sgn, uint32_t &nwin, uint32_t &nb, uint32_t &nb_top) {
   nwin = windows_of(c);
-  const uint32_t ctop = MSM_SCALAR_BITS - c * (nwin - 1);
+  const uint32_t shift = c * (nwin - 1);  // >= 222: (r-1) >> shift is r's top word shifted
+  const uint32_t ctop = MSM_SCALAR_BITS - shift;
   if (sgn) {
     nb = 1u << (c - 1);
-    nb_top = 1u << ctop;
+    nb_top = (uint32_t)std::min<uint64_t>(1ull << ctop, (R_WORDS[3] >> (shift - 192)) + 1);
   } else {
     nb = (1u << c) - 1;
     nb_top = (1u << ctop) - 1;
   }
+}
+
+// Sorted entries one point can produce: one per window, plus one when the top window's bucket
+// range is capped below 2^c_top (its digit then splits into nb_top and the rest, which is at most
+// nb_top since the cap is at least 2^(c_top - 1)).
+uint32_t entries_per_point(uint32_t c, uint32_t sgn) {
+  uint32_t nwin, nb, nbt;
+  layout(c, sgn, nwin, nb, nbt);
+  const uint32_t ctop = MSM_SCALAR_BITS - c * (nwin - 1);
+  return nwin + (sgn && nbt < (1u << ctop) ? 1u : 0u);
 }
 
 // Cost model in 12-limb products at throughput: 7 per bucket add, 18 per bucket in the
@@ -301,7 +319,7 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
       buckets += d.fixed ? (uint64_t)std::max(d.nb, d.nb_top)
                          : (uint64_t)(d.nwin - 1) * d.nb + d.nb_top;
       wins += d.nred;
-      pl.max_entries += s.n * d.nwin;
+      pl.max_entries += s.n * entries_per_point(d.c, d.signed_digits);
     }
     pl.n_points += s.n;
     pl.jobs.push_back(d);
@@ -314,10 +332,11 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
     return fail(ERR_BUDGET, "pass too large: %llu buckets, %llu entries",
                 (unsigned long long)buckets, (unsigned long long)pl.max_entries);
   pl.n_buckets = (uint32_t)buckets;
-  uint32_t max_nwin = 0;
-  for (const JobDesc &d : pl.jobs) max_nwin = std::max(max_nwin, d.nwin);
+  uint32_t max_epp = 0;  // entries per point
+  for (const JobDesc &d : pl.jobs)
+    if (d.nwin) max_epp = std::max(max_epp, entries_per_point(d.c, d.signed_digits));
   pl.n_chunks = (pl.n_points + MSM_POINTS_PER_CHUNK - 1) / MSM_POINTS_PER_CHUNK;
-  pl.stage_cap = MSM_POINTS_PER_CHUNK * max_nwin;
+  pl.stage_cap = MSM_POINTS_PER_CHUNK * max_epp;
   // MSM_SORT_RANGES=<n> overrides the number of key ranges of the staged sort (tests, tuning)
   const char *sr = getenv("MSM_SORT_RANGES");
   pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u);
@@ -570,6 +589,7 @@ int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
   if (stats_out) {
     stats_out[0] = cnt[CNT_TASKS];
     stats_out[1] = cnt[CNT_HEAVY];
+    stats_out[2] = cnt[CNT_ENTRIES];
   }
   if (cnt[CNT_ERROR]) {
     // the codes msm_pipeline.cu's kernels record (they skip the access that would be out of bounds)
@@ -705,7 +725,6 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
       return g_err;
     if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
     if (cx->timing) record_timings(cx, ws);
-    cx->last_stats[2] = pl.max_entries;
     cx->last_stats[3] = pl.n_buckets;
     memcpy(out, ws.res_host.p, m * MSM_PROJ_BYTES);
     return 0;
@@ -765,7 +784,6 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     if (cx->timing) {
       if (check_pass_errors(ws, cx->stream, cx->last_stats)) return g_err;
       record_timings(cx, ws);
-      cx->last_stats[2] = pl.max_entries;
       cx->last_stats[3] = pl.n_buckets;
     }
   }
@@ -841,13 +859,13 @@ uint32_t choose_fixed_base(uint64_t n) {
   budget = std::min(budget, (double)free_b - 16.0 * (1ull << 30));
   auto fits = [&](uint32_t c) {
     const uint32_t w = windows_of(c);
-    return w <= 24 && MSM_SCALAR_BITS % c != 0 && (double)n * w * MSM_BASE_BYTES <= budget &&
+    return w <= 24 && (double)n * w * MSM_BASE_BYTES <= budget &&
            (double)n * w < 2147483647.0;
   };
   if (e) {
     if (!strcmp(e, "0") || !strcmp(e, "off")) return 0;
     const int c = atoi(e);
-    if (c >= 11 && c <= 24 && MSM_SCALAR_BITS % c != 0 && windows_of(c) <= 24 &&
+    if (c >= 11 && c <= 24 && windows_of(c) <= 24 &&
         (double)n * windows_of(c) < 2147483647.0)
       return (uint32_t)c;
     if (strcmp(e, "auto")) return 0;
@@ -1023,8 +1041,6 @@ inline uint64_t rand_u64(uint64_t seed, uint64_t stream, uint64_t index, uint64_
   const uint64_t h = splitmix64(s ^ splitmix64(index));
   return splitmix64(h + word);
 }
-const uint64_t R_WORDS[4] = {0x0a11800000000001ull, 0x59aa76fed0000001ull, 0x60b44d1e5c37b001ull,
-                             0x12ab655e9a2ca556ull};
 inline bool lt_r(const uint64_t *v) {
   for (int k = 3; k >= 0; k--) {
     if (v[k] < R_WORDS[k]) return true;
@@ -1791,7 +1807,7 @@ extern "C" int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t 
     nsegs = (jd.nwin - 1) * nseg_low + nseg_top;
     ngrps = (jd.nwin - 1) * ((nseg_low + 511) / 512) + (nseg_top + 511) / 512;
   }
-  const uint64_t entries = n * jd.nwin;
+  const uint64_t entries = n * entries_per_point(jd.c, 1);
   const uint32_t tasks = (uint32_t)(nbk + entries / MSM_NOALLOC_SEG_LEN + 1);
   size_t off = 0;
   const size_t o_jobs = carve(off, sizeof(JobDesc));

@@ -89,9 +89,32 @@ __device__ __forceinline__ uint32_t bucket_key(const JobDesc &jd, uint32_t w, ui
   return jd.bucket_begin + (jd.fixed ? 0u : w * jd.nb) + (mag - 1u);
 }
 
+// The part of a digit's magnitude above its window's bucket range.  Only the top window of a
+// signed layout can have one: its range is capped at the largest top digit of a scalar below r,
+// and a 253-bit scalar at or above r can exceed it.  That digit becomes two entries of the same
+// window, nb_top and the excess (at most nb_top: the cap is at least half of 2^c_top).
+__device__ __forceinline__ uint32_t top_excess(const JobDesc &jd, uint32_t w, uint32_t mag) {
+  return (w + 1 == jd.nwin && mag > jd.nb_top) ? mag - jd.nb_top : 0u;
+}
+
 // ---------------------------------------------------------------------------------------------
 // 1. histogram
 // ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void count_key(const PassBuffers &pb, uint32_t key, uint32_t *sh_bins) {
+  if (sh_bins) atomicAdd(&sh_bins[key >> pb.bin_shift], 1u);
+  if (pb.stage_rank) return;  // the bucket counts come with the ranks in stage_digits
+  // a warp whose active lanes all hit one bucket (e.g. equal scalars) adds once; otherwise
+  // every lane adds on its own (distinct buckets for uniform scalars)
+  const uint32_t active = __activemask();
+  const int leader = __ffs(active) - 1;
+  const uint32_t k0 = __shfl_sync(active, key, leader);
+  if (__all_sync(active, key == k0)) {
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&pb.count[key], (uint32_t)__popc(active));
+  } else {
+    atomicAdd(&pb.count[key], 1u);
+  }
+}
+
 // Round 1: the global bucket histogram (and, for the staged sort, the block's key-range counts).
 __device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s,
                                              uint32_t *sh_bins) {
@@ -99,24 +122,42 @@ __device__ __forceinline__ void count_digits(const PassBuffers &pb, const JobDes
   for (uint32_t w = 0; w < jd.nwin; w++) {
     const int32_t d = next_digit(s, jd, w, carry);
     if (d == 0) continue;
-    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
-    if (sh_bins) atomicAdd(&sh_bins[key >> pb.bin_shift], 1u);
-    if (pb.stage_rank) continue;  // the bucket counts come with the ranks in stage_digits
-    // a warp whose active lanes all hit one bucket (e.g. equal scalars) adds once; otherwise
-    // every lane adds on its own (distinct buckets for uniform scalars)
-    const uint32_t active = __activemask();
-    const int leader = __ffs(active) - 1;
-    const uint32_t k0 = __shfl_sync(active, key, leader);
-    if (__all_sync(active, key == k0)) {
-      if ((int)(threadIdx.x & 31) == leader) atomicAdd(&pb.count[key], (uint32_t)__popc(active));
-    } else {
-      atomicAdd(&pb.count[key], 1u);
-    }
+    const uint32_t mag = (uint32_t)abs(d);
+    const uint32_t extra = top_excess(jd, w, mag);
+    count_key(pb, bucket_key(jd, w, mag - extra), sh_bins);
+    if (extra) count_key(pb, bucket_key(jd, w, extra), sh_bins);
   }
 }
 
-// Round 2 of the staged sort: the entries of one point into the block's chunk, at the cursors
-// of their key ranges.
+// Round 2 of the staged sort: one entry into the block's chunk, at the cursor of its key range.
+__device__ __forceinline__ void stage_key(const PassBuffers &pb, uint32_t key, uint32_t val,
+                                          uint32_t *sh_cur, uint2 *chunk, uint32_t *ranks) {
+  uint32_t rank = 0;
+  if (ranks) {
+    // the bucket count's old value is the entry's rank in its bucket (one atomic per warp
+    // when its active lanes share the bucket)
+    const uint32_t active = __activemask();
+    const int leader = __ffs(active) - 1;
+    const int lane = threadIdx.x & 31;
+    const uint32_t k0 = __shfl_sync(active, key, leader);
+    if (__all_sync(active, key == k0)) {
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&pb.count[key], (uint32_t)__popc(active));
+      rank = __shfl_sync(active, base, leader) + __popc(active & ((1u << lane) - 1u));
+    } else {
+      rank = atomicAdd(&pb.count[key], 1u);
+    }
+  }
+  const uint32_t pos = atomicAdd(&sh_cur[key >> pb.bin_shift], 1u);
+  if (pos < pb.stage_cap) {
+    chunk[pos] = make_uint2(key, val);
+    if (ranks) ranks[pos] = rank;
+  } else {
+    set_error(pb.counters, 6, pos);
+  }
+}
+
+// The entries of one point, in window order.
 __device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDesc &jd, ScalarBits s,
                                              uint64_t bidx, uint32_t *sh_cur, uint2 *chunk,
                                              uint32_t *ranks) {
@@ -124,32 +165,12 @@ __device__ __forceinline__ void stage_digits(const PassBuffers &pb, const JobDes
   for (uint32_t w = 0; w < jd.nwin; w++) {
     const int32_t d = next_digit(s, jd, w, carry);
     if (d == 0) continue;
-    const uint32_t key = bucket_key(jd, w, (uint32_t)abs(d));
+    const uint32_t mag = (uint32_t)abs(d);
+    const uint32_t extra = top_excess(jd, w, mag);
     const uint64_t tidx = jd.tab_base + (jd.fixed ? (uint64_t)w * jd.fb_stride : 0) + bidx;
     const uint32_t val = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
-    uint32_t rank = 0;
-    if (ranks) {
-      // the bucket count's old value is the entry's rank in its bucket (one atomic per warp
-      // when its active lanes share the bucket)
-      const uint32_t active = __activemask();
-      const int leader = __ffs(active) - 1;
-      const int lane = threadIdx.x & 31;
-      const uint32_t k0 = __shfl_sync(active, key, leader);
-      if (__all_sync(active, key == k0)) {
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&pb.count[key], (uint32_t)__popc(active));
-        rank = __shfl_sync(active, base, leader) + __popc(active & ((1u << lane) - 1u));
-      } else {
-        rank = atomicAdd(&pb.count[key], 1u);
-      }
-    }
-    const uint32_t pos = atomicAdd(&sh_cur[key >> pb.bin_shift], 1u);
-    if (pos < pb.stage_cap) {
-      chunk[pos] = make_uint2(key, val);
-      if (ranks) ranks[pos] = rank;
-    } else {
-      set_error(pb.counters, 6, pos);
-    }
+    stage_key(pb, bucket_key(jd, w, mag - extra), val, sh_cur, chunk, ranks);
+    if (extra) stage_key(pb, bucket_key(jd, w, extra), val, sh_cur, chunk, ranks);
   }
 }
 
@@ -294,6 +315,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_blocks(PassBuffers pb, ui
     if ((uint64_t)t.x > pb.max_entries) set_error(pb.counters, 1, t.x);
     if (t.y > pb.max_tasks) set_error(pb.counters, 2, t.y);
     pb.counters[CNT_TASKS] = min(t.y, pb.max_tasks);
+    pb.counters[CNT_ENTRIES] = t.x;
   }
 }
 
@@ -344,6 +366,8 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
   // four windows per step: their slot atomics are independent, so the four round trips
   // overlap instead of running one after another.  fill[key] starts at the bucket's offset in
   // the sorted array, so the atomic returns the entry's position directly.
+  uint32_t extra_key = 0, extra_val = 0;  // a split top digit's second entry (see top_excess)
+  bool extra = false;
 #pragma unroll 1
   for (uint32_t w0 = 0; w0 < jd.nwin; w0 += 4) {
     uint32_t key[4], val[4], pos[4];
@@ -357,11 +381,17 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
       if (w < jd.nwin) {
         const int32_t d = next_digit(s, jd, w, carry);
         if (d != 0) {
-          ok[k] = true;
-          key[k] = bucket_key(jd, w, (uint32_t)abs(d));
+          const uint32_t mag = (uint32_t)abs(d);
+          const uint32_t ex = top_excess(jd, w, mag);
+          key[k] = bucket_key(jd, w, mag - ex);
           ok[k] = key[k] >= key_lo && key[k] < key_hi;
           const uint64_t tidx = jd.tab_base + (jd.fixed ? (uint64_t)w * jd.fb_stride : 0) + bidx;
           val[k] = (uint32_t)tidx | (d < 0 ? 0x80000000u : 0u);
+          if (ex) {
+            extra_key = bucket_key(jd, w, ex);
+            extra_val = val[k];
+            extra = extra_key >= key_lo && extra_key < key_hi;
+          }
         }
       }
     }
@@ -389,6 +419,14 @@ __global__ void k_scatter(PassBuffers pb, uint32_t key_lo, uint32_t key_hi) {
       } else {
         set_error(pb.counters, 3, pos[k]);
       }
+    }
+  }
+  if (extra) {
+    const uint32_t p = atomicAdd(&pb.fill[extra_key], 1u);
+    if (p < pb.max_entries) {
+      pb.vals[p] = extra_val;
+    } else {
+      set_error(pb.counters, 3, p);
     }
   }
 }

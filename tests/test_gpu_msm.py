@@ -457,6 +457,38 @@ def test_width16_tables_on_a_large_context(engine, ocpu):
         ctx.close()
 
 
+@pytest.mark.parametrize("c", [23, 11])
+def test_fixed_base_top_window_cap(engine, ref, ocpu, c):
+    """The signed top window's buckets stop at the largest top digit of a scalar below r
+    (c = 23: 4894097 instead of 2^23).  Scalars up to 2^253 - 1, accepted as plain 253-bit
+    integers, can exceed it; such a top digit becomes two entries of the top window.  Edge
+    scalars sit at the cap, just above it and at the largest 253-bit values."""
+    nb = 2000
+    pts = ocpu.gen_bases(991, nb)
+    ctx = _ctx_with_fixed_base(engine, pts, c)
+    try:
+        nwin = -(-253 // c)
+        top = c * (nwin - 1)  # first bit of the top window
+        cap = ((ref.R_SCALAR - 1) >> top) + 1
+        rng = np.random.default_rng(c)
+        ks = [int.from_bytes(rng.bytes(32), "little") % ref.R_SCALAR for _ in range(nb)]
+        edge = [(1 << 253) - 1, ref.R_SCALAR - 1, 1 << 252, cap << top, (cap + 1) << top,
+                ((cap + 1) << top) - 1, (((1 << (253 - top)) - 1) << top) | ((1 << top) - 1) >> 1,
+                (1 << 253) - (1 << top), 1]
+        ks[:len(edge)] = edge
+        for i in range(len(edge), 300):  # 253-bit integers at or above r
+            ks[i] = ref.R_SCALAR + int.from_bytes(rng.bytes(32), "little") % ((1 << 253) - ref.R_SCALAR)
+        sc = scal(ref, ks)
+        for opts in (dict(fixed_base=1), dict(fixed_base=1, mode=2), dict(fixed_base=1, seg_len=8),
+                     dict(fixed_base=2), dict(fixed_base=2, window_bits=c)):
+            out = ctx.mult(sc, **opts)
+            assert np.array_equal(out[0], ocpu.msm(pts, sc)), opts
+            if opts == dict(fixed_base=1):  # nonzero digits, and the split top digits
+                assert nb * (nwin - 2) < ctx.last_pass_stats()["entries"] <= nb * (nwin + 1)
+    finally:
+        ctx.close()
+
+
 def test_fixed_base_with_even_order_bases(engine, ref, ocpu, kats):
     """The reference's second edge case holds a representable base of order 4, whose doubling
     chain reaches the order-two point (0, -1) and then the identity; the tables stay exact.  (A

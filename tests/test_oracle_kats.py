@@ -130,11 +130,19 @@ def test_signed_digit_split_reference_config(ref):
 def test_engine_digit_layout(ref):
     """The engine's uniform c-bit windows (sequential carry, as utils.ml:243-288): digits
     reconstruct the scalar, lower windows stay within 2^(c-1) buckets and the top window within
-    2^(253 - c (W-1)) buckets."""
+    2^(253 - c (W-1)) buckets.  The engine caps the signed top window's buckets at the largest
+    top digit of a scalar below r, floor((r-1) / 2^(c (W-1))) + 1, which is at least half of
+    2^(253 - c (W-1)): a larger top digit (a 253-bit scalar at or above r) splits into two
+    in-range entries."""
     rng = random.Random(5)
-    for c in (6, 10, 11, 13, 16, 20):
+    for c in (6, 10, 11, 13, 16, 20, 22, 23):
         sizes = ref.uniform_window_sizes(c)
         assert sum(sizes) == 253 and len(sizes) == -(-253 // c)
+        top_off = ref.offsets(sizes)[-1]
+        cap = ((ref.R_SCALAR - 1) >> top_off) + 1
+        assert 2 * cap >= 1 << sizes[-1] and cap <= 1 << sizes[-1]
+        for k in (ref.R_SCALAR - 1, rng.randrange(ref.R_SCALAR), (1 << top_off) - 1):
+            assert 0 <= ref.signed_digits(k, sizes)[-1] <= cap
         for _ in range(200):
             k = rng.getrandbits(253) if _ % 4 else (1 << 253) - 1 - rng.getrandbits(8)
             d = ref.signed_digits(k, sizes)
