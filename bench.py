@@ -272,7 +272,7 @@ def run_ours(args, rank, world, local):
     msm_s = t_dev / args.steps
     t_acc = stage_acc.get("accumulate", 0) * 1e-3
     entries = int(stats["entries"])  # mixed adds of one pass: its nonzero digits
-    w_tab = 253 // cfg["window_bits"] + 1  # signed windows: fixed-base tables per base
+    w_tab = -(-253 // cfg["window_bits"])  # windows: fixed-base tables per base
     acc_imad = entries * C_MADD
     achieved = acc_imad / t_acc if t_acc > 0 else None
     traffic = None

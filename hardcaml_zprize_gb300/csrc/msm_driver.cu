@@ -342,10 +342,12 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u);
   pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
   if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
-  // ranks from the histogram's atomics save the scatter's slot atomics; on GB300 that won for
-  // 2^27.6 and 2^26.7 entries (2^24 points, the uneven mix) and lost for 2^29.5 (2^26 points,
-  // whose 2^23 bucket counters made the returning atomics slow)
-  pl.ranks = pl.max_entries < (1ull << 29);
+  // ranks from the histogram's atomics save the scatter's slot atomics, but the histogram's
+  // atomics then return a value.  Measured on GB300 (count + scatter): the uneven 64-MSM mix
+  // (up to 1.0e8 entries, 2^21 buckets) 2.03 ms with ranks, 2.67 ms without; 2^24 points on
+  // tables of width 23 (2.0e8 entries, 4.9M buckets) 5.65 against 4.86; 2^26 points (8.1e8)
+  // 16.5 against 14.0
+  pl.ranks = pl.max_entries < (1ull << 27);
   snprintf(tmp, sizeof(tmp), "|r%u", pl.bin_shift);
   pl.key += tmp;
   pl.n_segs = (uint32_t)segs;
