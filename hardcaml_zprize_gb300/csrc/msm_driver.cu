@@ -136,14 +136,15 @@ struct Cfg {
                        // then the tables' width); 0: windowed over the plain bases
 };
 
-// Level-1 reduction runs of 2^red buckets, 8 to 64: passes of more than 2^21 buckets take
-// longer runs (about 2^17 of them still keep k_reduce1 at the product throughput), which leaves
-// fewer groups for the latency-bound level 2.  Measured on GB300: 8 is best at 2^15 buckets,
-// 16 at 2^21 (8 and 16 tie at 2^19), 32 at 4.8 M (the uneven 64-MSM mix), 64 at 2^23.
+// Level-1 reduction runs of 2^red buckets, 8 to 64: passes of 2^22 buckets or more take runs of
+// 64 (about 2^16 of them still keep k_reduce1 near the product throughput), which leaves fewer
+// groups for the latency-bound levels 2 and 3.  Measured on GB300: 8 is best at 2^15 buckets,
+// 16 at 2^21 (8 and 16 tie at 2^19); at 4.9 M shared buckets (tables of width 23) 64 beats 32
+// by 0.3 ms (level 1 +0.08 ms, levels 2 and 3 -0.37 ms), and 64 is best at 2^23.
 uint32_t red_log2_for(uint64_t buckets) {
   int lg = 0;
   while (lg < 63 && (2ull << lg) <= buckets) lg++;  // floor(log2(buckets))
-  return (uint32_t)std::min(6, std::max(lg <= 18 ? 3 : 4, lg - 17));
+  return lg <= 18 ? 3u : lg <= 21 ? 4u : 6u;
 }
 
 constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
