@@ -27,7 +27,8 @@ struct JobDesc {
   uint32_t c;             // window width in bits
   uint32_t nwin;          // number of windows
   uint32_t nb;            // buckets per window below the top one
-  uint32_t nb_top;        // buckets in the top window
+  uint32_t nb_top;        // buckets in the top window (signed: capped at the largest top digit
+                          // of a scalar below r; a larger digit is split into two entries)
   uint32_t bucket_begin;  // first global bucket id
   uint32_t win_begin;     // first global window id
   uint32_t signed_digits; // 1: signed c-bit digits, 0: unsigned
@@ -108,7 +109,7 @@ struct PassBuffers {
   uint32_t *stage_rank;         // or null: [n_chunks * stage_cap] each staged entry's rank in its
                                 // bucket, taken from the bucket count when the entry is staged
   uint32_t *blk_off;            // [n_chunks * (n_bins + 1)]
-  uint32_t stage_cap;           // entries per chunk: 256 x the pass's largest window count
+  uint32_t stage_cap;           // entries per chunk: 256 x the pass's most entries per point
   uint32_t bin_shift;           // key range of a bucket key
   uint32_t n_bins;              // key ranges (<= MSM_MAX_BINS)
 
