@@ -206,14 +206,23 @@ double model_cost_fixed(uint64_t n, uint32_t c, uint32_t sgn) {
   return (double)n * nwin * 7.0 + (double)std::max(nb, nbt) * 24.0;
 }
 
-// Longest run of entries one accumulate thread sums: twice the mean bucket load (buckets of
-// `nwin_sharing` windows), so most buckets stay whole, but short enough that the n x nwin
-// entries make at least ~2^17 runs: with few, heavily loaded buckets (a fixed-base table of
-// small width) whole-bucket runs would leave most of the GPU idle.
-uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing, uint32_t nwin) {
-  const double mean = (double)n * nwin_sharing / std::max<uint32_t>(nb, 1);
+// Run length that keeps buckets of mean load `mean` whole but for their Poisson tail: the
+// smallest power of two (32 to 4096) at or above mean + 2 sqrt(mean).  Measured on GB300 with
+// fixed-base tables: mean 26 (2^20 points, c = 20) 64 beats 32 and 128; mean 104 (2^22) 128
+// beats 64 (merges) and 256 (longer runs unbalance the warps) by 1%; means 38 and 151 (2^24,
+// 2^26 at c = 23) tie from 64 and 256 up.
+uint32_t whole_bucket_run(double mean) {
   uint32_t s = 32;
-  while (s < 2 * mean && s < 4096) s <<= 1;
+  while (s < mean + 2.0 * std::sqrt(mean) && s < 4096) s <<= 1;
+  return s;
+}
+
+// Longest run of entries one accumulate thread sums: whole buckets of `nwin_sharing` windows
+// but for the tail, and short enough that the n x nwin entries make at least ~2^17 runs: with
+// few, heavily loaded buckets (a fixed-base table of small width) whole-bucket runs would leave
+// most of the GPU idle.
+uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing, uint32_t nwin) {
+  const uint32_t s = whole_bucket_run((double)n * nwin_sharing / std::max<uint32_t>(nb, 1));
   const uint64_t entries = n * (uint64_t)nwin;
   uint32_t cap = 16;
   while (cap < 4096 && ((uint64_t)cap << 18) <= entries) cap <<= 1;  // entries / cap >= 2^17
@@ -264,8 +273,8 @@ struct Plan {
   std::string key;
 };
 
-// Run length of a pass of several MSMs: twice the largest mean bucket load among them (as
-// seg_len_for does for one MSM), capped so the whole pass makes at least 2^19 runs.  Each MSM's
+// Run length of a pass of several MSMs: whole buckets at the largest mean bucket load among them
+// (as seg_len_for does for one MSM), capped so the whole pass makes at least 2^19 runs.  Each MSM's
 // own choice is capped by its own entries and is too short in a shared pass.  Measured on GB300,
 // the uneven 64-MSM mix (1.1e8 entries, 10% of each MSM's scalars one repeated value) over a
 // 2^24-base context: runs of 64 (the largest MSM's own choice) 35.8 ms, 256 34.4 ms, 512 36.0 ms,
@@ -282,8 +291,7 @@ uint32_t pass_seg_len(const std::vector<JobSpec> &specs) {
     mean = std::max(mean, load);
     entries += sp.n * entries_per_point(sp.cfg.c, sp.cfg.signed_digits);
   }
-  uint32_t seg = 32;
-  while (seg < 2 * mean && seg < 4096) seg <<= 1;
+  const uint32_t seg = whole_bucket_run(mean);
   uint32_t cap = 16;
   while (cap < 4096 && ((uint64_t)cap << 19) <= entries) cap <<= 1;
   return std::min(seg, cap);
