@@ -38,6 +38,7 @@ EXPORTED = [
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
     "msm_mult_noalloc", "msm_measure_int_peaks", "msm_fq_to_montgomery", "msm_fq_from_montgomery",
     "msm_fr_to_montgomery", "msm_fr_from_montgomery",
+    "zprize_msm_fpga_init", "zprize_msm_fpga_mult", "zprize_msm_pippenger_mult",
 ]
 
 STAGES = ["count", "scan", "scatter", "tasks", "accumulate", "merge", "reduce1", "reduce2",
@@ -76,6 +77,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     sig = {
         "msm_init": (P, [P, ctypes.c_ssize_t, P, ctypes.c_ssize_t]),
         "msm_mult": (None, [P, P, U64, P]),
+        "zprize_msm_fpga_init": (P, [P, ctypes.c_ssize_t]),
+        "zprize_msm_fpga_mult": (None, [P, P, U64, P]),
+        "zprize_msm_pippenger_mult": (None, [P, P, U64, P]),
         "msm_last_error": (ctypes.c_int, [ctypes.c_char_p, SZ]),
         "msm_free": (None, [P]),
         "msm_mult_ex": (ctypes.c_int, [P, P, U64, P, ctypes.POINTER(MsmOptions)]),

@@ -1334,6 +1334,23 @@ void msm_mult(void *context, g1_projective_t *out, uint64_t batch_size,
     fprintf(stderr, "msm_mult: %s\n", g_msg);
 }
 
+// The naive driver's names for the same two calls (host/naive_driver/naive_driver.cpp:109-138),
+// which test_naive_harness binds.  There the "fpga" product is a CPU double-and-add loop and the
+// "pippenger" product a CPU Pippenger; both are the full MSM, as here.
+void *zprize_msm_fpga_init(const g1_affine_t *points, ssize_t npoints) {
+  return msm_init(nullptr, 0, points, npoints);
+}
+
+void zprize_msm_fpga_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+                          const biginteger256_t *scalars) {
+  msm_mult(context, out, batch_size, scalars);
+}
+
+void zprize_msm_pippenger_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+                               const biginteger256_t *scalars) {
+  msm_mult(context, out, batch_size, scalars);
+}
+
 int msm_mult_uneven(void *context, g1_projective_t *out, uint64_t num_msms, const uint64_t *sizes,
                     const uint64_t *base_offsets, const biginteger256_t *scalars,
                     const msm_options_t *opt) {

@@ -70,6 +70,18 @@ void *msm_init(const char *xclbin, ssize_t xclbin_len, const g1_affine_t *points
 void msm_mult(void *context, g1_projective_t *out, uint64_t batch_size,
               const biginteger256_t *scalars);
 
+/* The naive driver's names for the same two calls (zprize/msm_pippenger/host/naive_driver/
+ * naive_driver.cpp:109-138, bound by test_naive_harness/src/lib.rs:16-37):
+ * `zprize_msm_fpga_init(points, npoints)` is msm_init without the bitstream arguments, and
+ * `zprize_msm_fpga_mult` / `zprize_msm_pippenger_mult(ctx, out, batch_size, scalars)` are
+ * msm_mult.  In the reference they run a CPU double-and-add and a CPU Pippenger; both compute
+ * the same MSMs. */
+void *zprize_msm_fpga_init(const g1_affine_t *points, ssize_t npoints);
+void zprize_msm_fpga_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+                          const biginteger256_t *scalars);
+void zprize_msm_pippenger_mult(void *context, g1_projective_t *out, uint64_t batch_size,
+                               const biginteger256_t *scalars);
+
 /* ---------------------------------------------------------------------------------------------
  * Additions (no counterpart in the reference unless stated)
  * ------------------------------------------------------------------------------------------- */

@@ -130,6 +130,25 @@ def test_msm_knobs(engine, ocpu, opts):
         ctx.close()
 
 
+def test_naive_driver_entry_points(engine, ocpu):
+    """The naive driver's names (naive_driver.cpp:109-138) bind the same context and MSMs."""
+    import ctypes
+    lib = engine.load_library()
+    n = 700
+    pts = ocpu.gen_bases(55, n)
+    sc = engine.generate_scalars(56, 3 * n)
+    ctx = lib.zprize_msm_fpga_init(pts.ctypes.data, n)
+    assert ctx
+    try:
+        for fn in (lib.zprize_msm_pippenger_mult, lib.zprize_msm_fpga_mult):
+            out = np.zeros((3, engine.PROJ_BYTES), dtype=np.uint8)
+            fn(ctypes.c_void_p(ctx), out.ctypes.data, 3, sc.ctypes.data)
+            for b in range(3):
+                assert np.array_equal(out[b], ocpu.msm(pts, sc[b * n:(b + 1) * n])), (fn, b)
+    finally:
+        lib.msm_free(ctypes.c_void_p(ctx))
+
+
 def test_trivial_inputs(engine, ref, ocpu):
     """TEST_TRIVIAL_INPUTS of the harness (util.rs:164-183): all bases G, scalar[0] = 1."""
     n = 256
