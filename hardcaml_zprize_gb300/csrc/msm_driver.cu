@@ -147,7 +147,6 @@ uint32_t red_log2_for(uint64_t buckets) {
   return lg <= 18 ? 3u : lg <= 21 ? 4u : 6u;
 }
 
-constexpr uint32_t kGrpLenLog2 = 9;  // level-2 reduction group: 512 level-1 runs
 
 // the scalar field's modulus r, little-endian 64-bit words
 const uint64_t R_WORDS[4] = {0x0a11800000000001ull, 0x59aa76fed0000001ull, 0x60b44d1e5c37b001ull,
@@ -264,7 +263,7 @@ struct Plan {
   std::vector<WinDesc> wins;
   uint64_t n_points = 0, max_entries = 0;
   uint32_t n_buckets = 0, n_segs = 0, n_grps = 0, max_tasks = 0;
-  uint32_t seg_len = 1024, red_log2 = 5;
+  uint32_t seg_len = 1024, red_log2 = 5, grp_log2 = 9;
   // staged sort: histogram chunks of MSM_POINTS_PER_CHUNK points, each with room for the
   // largest window count of the pass, and the key ranges of the scatter
   uint64_t n_chunks = 0;
@@ -312,6 +311,29 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
     }
     pl.red_log2 = red_log2_for(total);
   }
+  // Level-2 groups of 2^grp_log2 level-1 runs.  A pass whose reduction is one window (one MSM on
+  // fixed-base tables) takes groups of 128 to 512 runs, about 128 groups: level 3 then combines
+  // enough groups to use a block (a window of at most 16 groups is combined serially by one
+  // quad) and few enough to keep its tree shallow.  Measured on GB300 (ms per MSM, groups of
+  // 512 / 256 / 128 runs): 2^12 and 2^16 points (4096 runs) 0.973 / 0.993 / 0.850 and 1.427 /
+  // 1.448 / 1.300; 2^20 (32 K runs) 6.290 / 6.219 / 6.307; 2^24 (76 K runs) 71.58 / 71.79 / 72.10.
+  // Passes of many windows (windowed MSMs, batches) keep groups of 512: the uneven 64-MSM mix
+  // (64 windows of 2048 runs) took 34.44 ms with them and 34.99 ms with groups of 128, whose
+  // 1024 level-2 blocks run in several waves.
+  {
+    uint32_t n_windows = 0;
+    uint64_t max_nb = 0;
+    for (const JobSpec &s : specs) {
+      if (s.n == 0) continue;
+      uint32_t nwin, nb, nbt;
+      layout(s.cfg.c, s.cfg.signed_digits, nwin, nb, nbt);
+      n_windows += s.cfg.fixed ? 1 : nwin;
+      max_nb = std::max<uint64_t>(max_nb, std::max(nb, nbt));
+    }
+    const uint64_t max_nseg = (max_nb + (1ull << pl.red_log2) - 1) >> pl.red_log2;
+    pl.grp_log2 = n_windows == 1 ? 7 : 9;
+    while (pl.grp_log2 < 9 && (max_nseg >> pl.grp_log2) > 128) pl.grp_log2++;
+  }
   uint64_t buckets = 0, segs = 0, wins = 0, grps = 0;
   char tmp[160];
   for (size_t j = 0; j < specs.size(); j++) {
@@ -345,7 +367,7 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
         wd.seg_begin = (uint32_t)segs;
         wd.nseg = (wd.nb + L - 1) / L;
         wd.grp_begin = (uint32_t)grps;
-        wd.ngrp = (wd.nseg + (1u << kGrpLenLog2) - 1) >> kGrpLenLog2;
+        wd.ngrp = (wd.nseg + (1u << pl.grp_log2) - 1) >> pl.grp_log2;
         segs += wd.nseg;
         grps += wd.ngrp;
         pl.wins.push_back(wd);
@@ -389,7 +411,7 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   const uint64_t mt = buckets + pl.max_entries / pl.seg_len + 1;
   if (mt >= (1ull << 31)) return fail(ERR_BUDGET, "too many tasks");
   pl.max_tasks = (uint32_t)mt;
-  snprintf(tmp, sizeof(tmp), "|%u|%u", pl.seg_len, pl.red_log2);
+  snprintf(tmp, sizeof(tmp), "|%u|%u|g%u", pl.seg_len, pl.red_log2, pl.grp_log2);
   pl.key += tmp;
   return 0;
 }
@@ -539,7 +561,7 @@ PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void
   pb.n_grps = pl.n_grps;
   pb.seg_len = pl.seg_len;
   pb.red_len_log2 = pl.red_log2;
-  pb.grp_len_log2 = kGrpLenLog2;
+  pb.grp_len_log2 = pl.grp_log2;
   pb.max_entries = pl.max_entries;
   pb.max_tasks = pl.max_tasks;
   pb.count = ws.count.as<uint32_t>();
