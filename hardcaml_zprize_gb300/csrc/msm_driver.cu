@@ -136,15 +136,19 @@ struct Cfg {
                        // then the tables' width); 0: windowed over the plain bases
 };
 
-// Level-1 reduction runs of 2^red buckets, 8 to 64: passes of 2^22 buckets or more take runs of
-// 64 (about 2^16 of them still keep k_reduce1 near the product throughput), which leaves fewer
-// groups for the latency-bound levels 2 and 3.  Measured on GB300: 8 is best at 2^15 buckets,
-// 16 at 2^21 (8 and 16 tie at 2^19); at 4.9 M shared buckets (tables of width 23) 64 beats 32
-// by 0.3 ms (level 1 +0.08 ms, levels 2 and 3 -0.37 ms), and 64 is best at 2^23.
+// Level-1 reduction runs of 2^red buckets, 4 to 64.  Small passes are latency-bound: each thread
+// adds 2 x 2^red points in sequence.  Passes of 2^22 buckets or more take runs of 64 (about 2^16
+// of them still keep k_reduce1 near the product throughput), which leaves fewer groups for the
+// latency-bound levels 2 and 3.  Measured on GB300:
+//   2^15 buckets (one MSM on tables of width 16): 4 beats 8 by 0.1 ms (2^12 points: 0.76 against
+//   0.87 ms per MSM), and 16 is 0.33 ms worse;
+//   2^21 buckets: 16 is best (8 and 16 tie at 2^19);
+//   4.9 M shared buckets (tables of width 23): 64 beats 32 by 0.3 ms (level 1 +0.08 ms, levels 2
+//   and 3 -0.37 ms), and 64 is best at 2^23.
 uint32_t red_log2_for(uint64_t buckets) {
   int lg = 0;
   while (lg < 63 && (2ull << lg) <= buckets) lg++;  // floor(log2(buckets))
-  return lg <= 18 ? 3u : lg <= 21 ? 4u : 6u;
+  return lg <= 15 ? 2u : lg <= 18 ? 3u : lg <= 21 ? 4u : 6u;
 }
 
 
