@@ -432,6 +432,23 @@ def test_staged_sort_key_ranges(engine, ocpu, monkeypatch, ranges):
             ctx.close()
 
 
+def test_all_equal_scalars_large(engine, ref, ocpu):
+    """2^18 equal scalars: every window's entries land in one bucket (2^18 entries, thousands of
+    runs merged by blocks of quads); once a random value, once r - 1 (every digit at its most
+    negative)."""
+    n = 1 << 18
+    pts = ocpu.gen_bases(4242, n)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        for k in (ref.uniform_scalar(4243, 0), ref.R_SCALAR - 1):
+            sc = np.repeat(scal(ref, [k]), n, axis=0)
+            out = ctx.mult(sc)
+            assert np.array_equal(out[0], ocpu.msm(pts, sc)), k
+            assert ctx.last_pass_stats()["heavy_buckets"] > 0
+    finally:
+        ctx.close()
+
+
 @pytest.mark.parametrize("seg_len", [512, 128, 32, 8])
 def test_merge_tiers(engine, ocpu, seg_len):
     """A bucket split into few, tens or hundreds of runs is merged by a thread, a warp or a block
