@@ -508,43 +508,61 @@ __global__ void k_len_scan(PassBuffers pb) {
   }
 }
 
-__global__ void k_tasks(PassBuffers pb) {
+// One thread per bucket writes the bucket's runs and their slots in the processing order: the
+// last run takes a slot in the bin of its length, the full runs of a split bucket a block of
+// slots in the seg_len bin.  The block ranks its runs per bin in shared memory and reserves each
+// bin's slots with one global atomic, so the few hot bin cursors (lengths cluster around the mean
+// bucket load) see one atomic per block and bin.
+__global__ void __launch_bounds__(256) k_tasks(PassBuffers pb) {
+  extern __shared__ uint32_t sh_bins[];  // [seg_len + 1] counts, then [seg_len + 1] slot bases
+  uint32_t *bin_cnt = sh_bins, *bin_base = sh_bins + pb.seg_len + 1;
+  for (uint32_t i = threadIdx.x; i <= pb.seg_len; i += blockDim.x) bin_cnt[i] = 0;
+  __syncthreads();
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= pb.n_buckets) return;
-  if (pb.counters[CNT_ERROR]) return;
-  const uint32_t cnt = pb.count[b];
-  if (cnt == 0) return;
-  const uint32_t nt = ntask_of(cnt, pb.seg_len);
-  const uint32_t t0 = pb.taskoff[b];
-  const uint32_t off = pb.offset[b];
-  if (t0 + nt > pb.max_tasks) {
-    set_error(pb.counters, 4, t0 + nt);
-    return;
+  bool live = b < pb.n_buckets && !pb.counters[CNT_ERROR];
+  uint32_t cnt = 0, nt = 0, t0 = 0, last = 0, r_last = 0, r_full = 0;
+  if (live) {
+    cnt = pb.count[b];
+    live = cnt != 0;
   }
-  for (uint32_t k = 0; k < nt; k++) {
-    Task tk;
-    tk.start = off + k * pb.seg_len;
-    tk.len = min(pb.seg_len, cnt - k * pb.seg_len);
-    tk.bucket = b;
-    tk.pad = 0;
-    pb.tasks[t0 + k] = tk;
+  if (live) {
+    nt = ntask_of(cnt, pb.seg_len);
+    t0 = pb.taskoff[b];
+    if (t0 + nt > pb.max_tasks) {
+      set_error(pb.counters, 4, t0 + nt);
+      live = false;
+    }
   }
-  // processing order: full runs reserve a block of slots in the seg_len bin, the last run one
-  // slot in the bin of its length (warp-aggregated)
-  if (nt > 1) {
-    const uint32_t base = atomicAdd(&pb.len_hist[pb.seg_len], nt - 1);
-    for (uint32_t k = 0; k + 1 < nt; k++) pb.order[base + k] = t0 + k;
-    pb.heavy[atomicAdd(&pb.counters[CNT_HEAVY], 1u)] = b;
+  if (live) {
+    const uint32_t off = pb.offset[b];
+    for (uint32_t k = 0; k < nt; k++) {
+      Task tk;
+      tk.start = off + k * pb.seg_len;
+      tk.len = min(pb.seg_len, cnt - k * pb.seg_len);
+      tk.bucket = b;
+      tk.pad = 0;
+      pb.tasks[t0 + k] = tk;
+    }
+    last = cnt - (nt - 1) * pb.seg_len;
+    r_last = atomicAdd(&bin_cnt[last], 1u);
+    if (nt > 1) {
+      r_full = atomicAdd(&bin_cnt[pb.seg_len], nt - 1);
+      pb.heavy[atomicAdd(&pb.counters[CNT_HEAVY], 1u)] = b;
+    }
   }
-  const uint32_t last = cnt - (nt - 1) * pb.seg_len;
-  const uint32_t active = __activemask();
-  const uint32_t peers = __match_any_sync(active, last);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  uint32_t pos = 0;
-  if (lane == leader) pos = atomicAdd(&pb.len_hist[last], (uint32_t)__popc(peers));
-  pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
-  pb.order[pos] = t0 + nt - 1;
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i <= pb.seg_len; i += blockDim.x) {
+    const uint32_t c = bin_cnt[i];
+    bin_base[i] = c ? atomicAdd(&pb.len_hist[i], c) : 0u;
+  }
+  __syncthreads();
+  if (live) {
+    if (nt > 1) {
+      const uint32_t base = bin_base[pb.seg_len] + r_full;
+      for (uint32_t k = 0; k + 1 < nt; k++) pb.order[base + k] = t0 + k;
+    }
+    pb.order[bin_base[last] + r_last] = t0 + nt - 1;
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1190,7 +1208,7 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
     launched++;
     k_len_scan<<<1, 32, 0, st>>>(pb);
     launched++;
-    k_tasks<<<(pb.n_buckets + 255) / 256, 256, 0, st>>>(pb);
+    k_tasks<<<(pb.n_buckets + 255) / 256, 256, 2 * (pb.seg_len + 1) * 4, st>>>(pb);
     launched++;
   }
   mark(4);
