@@ -9,6 +9,7 @@ links, ``cargo:rustc-link-lib=dylib=driver``).  Objects go to hardcaml_zprize_gb
 """
 from __future__ import annotations
 
+import fcntl
 import os
 import shutil
 import subprocess
@@ -38,7 +39,16 @@ def _newer(target: str, deps) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
+    """Compile and link libdriver.so when a source or header is newer than it.  Processes that
+    build at once (one per rank under torchrun) take turns on a lock file, so none links or loads
+    a half-written object."""
     os.makedirs(BUILD, exist_ok=True)
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        return _build_locked(verbose, force)
+
+
+def _build_locked(verbose: bool, force: bool) -> str:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(PKG, "..", "include", "msm_gb300.h"))
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]

@@ -20,12 +20,13 @@ def build(force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
+    tmp = f"{LIB}.{os.getpid()}.tmp"  # one file per builder; the rename below is atomic
     cmd = [os.environ.get("CC", "gcc"), "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", SRC,
-           "-o", LIB + ".tmp"]
+           "-o", tmp]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{p.stdout}\n{p.stderr}")
-    os.replace(LIB + ".tmp", LIB)
+    os.replace(tmp, LIB)
     return LIB
 
 
