@@ -142,7 +142,7 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t str
 #define MSM_NUM_STAGES 10
 size_t msm_scan_tmp_words(uint32_t n_buckets);
 uint32_t msm_scatter_passes(uint64_t max_entries);
-uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries, uint32_t ranges);
+uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries, uint32_t ranges, bool cursors);
 uint64_t msm_upload_chunk_points(uint64_t n_points, int nchunks);
 
 // resident-base preparation

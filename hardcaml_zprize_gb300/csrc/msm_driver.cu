@@ -399,15 +399,16 @@ int build_plan(const std::vector<JobSpec> &specs, Plan &pl) {
   pl.stage_cap = MSM_POINTS_PER_CHUNK * max_epp;
   // MSM_SORT_RANGES=<n> overrides the number of key ranges of the staged sort (tests, tuning)
   const char *sr = getenv("MSM_SORT_RANGES");
-  pl.bin_shift = msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u);
-  pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
-  if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
   // ranks from the histogram's atomics save the scatter's slot atomics, but the histogram's
   // atomics then return a value.  Measured on GB300 (count + scatter): the uneven 64-MSM mix
   // (up to 1.0e8 entries, 2^21 buckets) 2.03 ms with ranks, 2.67 ms without; 2^24 points on
-  // tables of width 23 (2.0e8 entries, 4.9M buckets) 5.65 against 4.86; 2^26 points (8.1e8)
-  // 16.5 against 14.0
+  // tables of width 23 (2.0e8 entries, 4.9M buckets) 5.65 against 4.86 with ranges of 2^20 keys,
+  // and the cursors 3.45 with ranges of 2^19 keys; 2^26 points (8.1e8) 16.5 against 14.0
   pl.ranks = pl.max_entries < (1ull << 27);
+  pl.bin_shift =
+      msm_bin_shift(pl.n_buckets, pl.max_entries, sr ? (uint32_t)atoi(sr) : 0u, !pl.ranks);
+  pl.n_bins = pl.n_buckets ? ((pl.n_buckets - 1) >> pl.bin_shift) + 1 : 0;
+  if (pl.n_bins > MSM_MAX_BINS) return fail(ERR_STATE, "too many key ranges: %u", pl.n_bins);
   snprintf(tmp, sizeof(tmp), "|r%u", pl.bin_shift);
   pl.key += tmp;
   pl.n_segs = (uint32_t)segs;

@@ -1124,16 +1124,22 @@ uint32_t msm_scatter_passes(uint64_t max_entries) {
   return (uint32_t)(p < 1 ? 1 : p > 8 ? 8 : p);
 }
 
-// Key ranges of the staged sort: one per ~150 MB of sorted array, as a shift of the bucket key
-// (ranges of 2^shift keys, at most MSM_MAX_BINS of them).  On GB300 the best counts measured
-// were 4 ranges for 2^24 points x 12 windows and 16 for 2^26 x 11 windows.
+// Key ranges of the staged sort, as a shift of the bucket key (ranges of 2^shift keys, at most
+// MSM_MAX_BINS of them): one per ~150 MB of sorted array, and, for a scatter with slot cursors,
+// no more than 2^19 keys per range while that keeps MSM_MAX_BINS ranges or fewer.  The keys a
+// scatter launch touches bound its slot-cursor footprint: measured on GB300 at 2^24 points (4.9 M buckets), ranges of 2^20 keys
+// (5 launches) took 3.86 ms, 2^19 (10) 2.42 ms and 2^18 (19) 2.49 ms; 2^26 points use 2^18.
 // `ranges` > 0 asks for that many ranges instead (rounded to a shift).
-uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries, uint32_t ranges) {
+uint32_t msm_bin_shift(uint32_t n_buckets, uint64_t max_entries, uint32_t ranges, bool cursors) {
   const uint64_t per = 150ull << 20;
   const uint64_t want = ranges ? ranges : (max_entries * 4 + per / 2) / per;
   const uint32_t target = (uint32_t)(want < 1 ? 1 : want > MSM_MAX_BINS ? MSM_MAX_BINS : want);
   uint32_t shift = 0;
   while (shift < 31 && (((uint64_t)n_buckets + (1ull << shift) - 1) >> shift) > target) shift++;
+  if (!ranges && cursors)
+    while (shift > 19 &&
+           (((uint64_t)n_buckets + (1ull << (shift - 1)) - 1) >> (shift - 1)) <= MSM_MAX_BINS)
+      shift--;
   return shift;
 }
 
