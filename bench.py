@@ -168,12 +168,11 @@ def run_reference(args, rank, world):
     """Reference arm: the CPU port of the oracle algorithm on all host cores."""
     if rank != 0:
         return
-    import hardcaml_zprize_gb300 as eng
-    from oracle import cpu as ocpu
+    from oracle import cpu as ocpu  # this arm loads the oracle library and nothing of the engine
     n = 1 << args.log2n
     cores = os.cpu_count() or 1
     pts = ocpu.gen_bases(args.seed, n, threads=cores)
-    sc = eng.generate_scalars(args.seed + 1, n)
+    sc = ocpu.gen_scalars(args.seed + 1, n, threads=cores)  # the engine's draws for this seed
     # warm-up steps page in the code and the inputs on a 2^16-point slice; every timed step is a
     # full MSM of the configured size (about 15 s at 2^24 on 16 Grace cores)
     nw = min(n, 1 << 16)
@@ -447,14 +446,31 @@ def run_fixed_base_large(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
-def bench_batched(args, eng, ctx, torch, dev):
-    rng = np.random.default_rng(args.seed + 7)
-    nbase = 1 << 20
-    m = 64
+def uneven_mix(seed: int, gen_scalars, m: int = 64, nbase: int = 1 << 20):
+    """The uneven batch: m MSMs of sizes floor(2^U), U ~ U[10, 20], each over a slice of a shared
+    base set of nbase bases, scalars of the mix (70% uniform 253-bit, 10% 16-bit, 10% 0 or r - 1,
+    10% one repeated value per MSM).  Returns (sizes, offsets, concatenated scalars)."""
+    rng = np.random.default_rng(seed + 7)
     sizes = [int(2 ** u) for u in rng.uniform(10, 20, m)]
     offs = [int(rng.integers(0, nbase - s + 1)) for s in sizes]
-    sc = np.concatenate([eng.generate_scalars(args.seed + 11, s, kind=1, msm_index=j)
-                         for j, s in enumerate(sizes)])
+    sc = np.concatenate([gen_scalars(seed + 11, s, kind=1, msm_index=j) for j, s in enumerate(sizes)])
+    return sizes, offs, sc
+
+
+def served_mix(seed: int, gen_scalars, m: int, nbase: int = 1 << 22):
+    """The served requests: m requests of sizes floor(2^U), U ~ U[12, 22], over slices of a
+    base set of nbase bases, uniform 253-bit scalars.  Returns (rng, sizes, offsets, scalars)."""
+    rng = np.random.default_rng(seed + 9)
+    sizes = [int(2 ** u) for u in rng.uniform(12, 22, m)]
+    offs = [int(rng.integers(0, nbase - s + 1)) for s in sizes]
+    reqs = [gen_scalars(seed + 100 + j, s) for j, s in enumerate(sizes)]
+    return rng, sizes, offs, reqs
+
+
+def bench_batched(args, eng, ctx, torch, dev):
+    nbase = 1 << 20
+    m = 64
+    sizes, offs, sc = uneven_mix(args.seed, eng.generate_scalars, m, nbase)
     dsc = torch.from_numpy(sc.view(np.uint8).reshape(-1)).to(dev)
     torch.cuda.synchronize()
     res = {}
@@ -504,12 +520,9 @@ def bench_batched(args, eng, ctx, torch, dev):
 
 
 def bench_served(args, eng, ctx, n):
-    rng = np.random.default_rng(args.seed + 9)
     nbase = min(n, 1 << 22)
     m = args.served_requests
-    sizes = [int(2 ** u) for u in rng.uniform(12, 22, m)]
-    offs = [int(rng.integers(0, nbase - s + 1)) for s in sizes]
-    reqs = [eng.generate_scalars(args.seed + 100 + j, s) for j, s in enumerate(sizes)]
+    rng, sizes, offs, reqs = served_mix(args.seed, eng.generate_scalars, m, nbase)
     # plain: one request at a time
     t0 = time.perf_counter()
     plain_out = [ctx.mult_uneven([s], [o], r)[0] for s, o, r in zip(sizes, offs, reqs)]

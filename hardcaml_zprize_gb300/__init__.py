@@ -32,7 +32,7 @@ SCALAR_BYTES = 32
 # every symbol include/msm_gb300.h declares
 EXPORTED = [
     "msm_init", "msm_mult", "msm_last_error", "msm_free", "msm_mult_ex", "msm_mult_uneven",
-    "msm_mult_device", "msm_get_config", "msm_tune", "msm_set_timing", "msm_last_timings",
+    "msm_mult_device", "msm_get_config", "msm_context_info", "msm_tune", "msm_set_timing", "msm_last_timings",
     "msm_last_pass_stats", "msm_server_create", "msm_server_submit", "msm_server_poll",
     "msm_server_stats", "msm_server_destroy", "msm_generate_bases", "msm_generate_scalars",
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
@@ -86,6 +86,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "msm_mult_uneven": (ctypes.c_int, [P, P, U64, P, P, P, ctypes.POINTER(MsmOptions)]),
         "msm_mult_device": (ctypes.c_int, [P, P, U64, P, P, P, ctypes.POINTER(MsmOptions)]),
         "msm_get_config": (ctypes.c_int, [P, U64, ctypes.POINTER(MsmOptions)]),
+        "msm_context_info": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64), I32]),
         "msm_tune": (ctypes.c_int, [P, U64, I32, ctypes.POINTER(MsmOptions)]),
         "msm_set_timing": (ctypes.c_int, [P, I32]),
         "msm_last_timings": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double), I32]),
@@ -213,6 +214,16 @@ class MultiScalarMultContext:
         o = MsmOptions()
         _check(load_library().msm_get_config(self.handle, n, ctypes.byref(o)), "msm_get_config")
         return {f: getattr(o, f) for f, _ in MsmOptions._fields_}
+
+    def info(self) -> dict:
+        """What the context keeps resident: bases, bytes of base records, table sets."""
+        arr = (ctypes.c_uint64 * 6)()
+        k = load_library().msm_context_info(self.handle, arr, 6)
+        if k < 0:
+            raise MsmError(f"msm_context_info: {last_error()}")
+        keys = ["npoints", "resident_bytes", "table_bits", "table_windows", "table2_bits",
+                "table2_windows"]
+        return {keys[i]: int(arr[i]) for i in range(k)}
 
     def tune(self, n: int, budget_ms: int = 0) -> dict:
         o = MsmOptions()

@@ -1429,6 +1429,16 @@ int msm_get_config(void *context, uint64_t npoints, msm_options_t *out) {
   return 0;
 }
 
+int msm_context_info(void *context, uint64_t *info, int32_t max_info) {
+  auto *cx = (Ctx *)context;
+  if (!cx || !info) return fail(ERR_ARG, "msm_context_info: null argument");
+  const uint64_t v[6] = {cx->npoints, (uint64_t)cx->bases.bytes, cx->fb_c, cx->fb_c ? cx->fb_w : 0,
+                         cx->fb2_c, cx->fb2_c ? cx->fb2_w : 0};
+  const int32_t k = std::min<int32_t>(max_info, 6);
+  for (int32_t i = 0; i < k; i++) info[i] = v[i];
+  return k;
+}
+
 int msm_set_timing(void *context, int32_t enable) {
   auto *cx = (Ctx *)context;
   if (!cx) return fail(ERR_ARG, "null context");

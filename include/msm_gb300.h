@@ -127,6 +127,12 @@ int msm_get_config(void *context, uint64_t npoints, msm_options_t *out);
  * the time spent (0: default). Returns 0 and fills `best` (may be NULL). */
 int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *best);
 
+/* What a context keeps resident: number of bases, bytes of the base records (the 144 B plain
+ * records, or every fixed-base table record), main table width and windows (0 and 0 without
+ * tables), second table set width and windows (0 and 0 when absent). Returns the number of
+ * values written (at most 6). */
+int msm_context_info(void *context, uint64_t *info, int32_t max_info);
+
 /* Per-stage device times (ms, CUDA events on the pipeline stream) of the last pass when timing
  * is enabled with msm_set_timing(ctx, 1). Stage order: count, scan, scatter, tasks, accumulate,
  * merge, reduce1, reduce2, reduce3, final. Returns the number of stages written. */
@@ -146,7 +152,11 @@ int msm_last_pass_stats(void *context, uint64_t *stats, int32_t max_stats);
  * is rejected with an error).  The first call on a device looks up that array's address, so
  * make the first call before any stream capture.  The call only enqueues work on `stream`
  * (NULL: the legacy default stream); synchronise it before reading `d_out`.  All calls share
- * the array: calls that overlap on the GPU race, so order them (for example on one stream). */
+ * the array: calls that overlap on the GPU race, so order them (for example on one stream).
+ * The array's address is looked up once per device and kept for the life of the process, so do
+ * not keep using the library on a device after cudaDeviceReset.  The return code covers the
+ * arguments and the launches only: when a device bounds check stops the MSM, `d_out` receives
+ * 144 zero bytes, which no result can be (the zero point is written as (R, R, 0)). */
 int msm_mult_noalloc(void *context, g1_projective_t *d_out, uint64_t n, uint64_t base_offset,
                      const biginteger256_t *d_scalars, void *stream);
 

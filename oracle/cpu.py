@@ -34,6 +34,8 @@ def lib():
         L.oracle_default_window.restype = I
         L.oracle_rand_u64.argtypes = [U64, U64, U64, U64]
         L.oracle_rand_u64.restype = U64
+        L.oracle_gen_scalars.argtypes = [U64, U64, I, U64, P, I]
+        L.oracle_gen_scalars.restype = I
         _lib = L
     return _lib
 
@@ -51,6 +53,15 @@ def msm(points: np.ndarray, scalars: np.ndarray, c: int = 0, threads: int = 0) -
 def gen_bases(seed: int, n: int, first: int = 0, threads: int = 0) -> np.ndarray:
     out = np.zeros((n, 104), dtype=np.uint8)
     lib().oracle_gen_bases(seed, first, n, out.ctypes.data, threads)
+    return out
+
+
+def gen_scalars(seed: int, n: int, kind: int = 0, msm_index: int = 0, threads: int = 0) -> np.ndarray:
+    """Seeded scalars as (n, 4) uint64: kind 0 uniform in [0, r), kind 1 the uneven-batch mix of
+    MSM `msm_index` (the draws of oracle/bls12_377.py uniform_scalar / mixed_scalar)."""
+    out = np.zeros((n, 4), dtype=np.uint64)
+    if lib().oracle_gen_scalars(seed, n, kind, msm_index, out.ctypes.data, threads) != 0:
+        raise ValueError(f"unknown scalar kind {kind}")
     return out
 
 

@@ -382,3 +382,57 @@ int oracle_mul(const void *point, const uint64_t *k, uint64_t *out) {
   store_proj(&acc, out);
   return 0;
 }
+
+/* ---- seeded scalars (the same SplitMix64 draws as oracle/bls12_377.py uniform_scalar and
+ *      mixed_scalar), so the CPU baseline makes its inputs without the engine ---- */
+static const uint64_t R_SCALAR_WORDS[4] = {0x0a11800000000001ull, 0x59aa76fed0000001ull,
+                                           0x60b44d1e5c37b001ull, 0x12ab655e9a2ca556ull};
+static int lt_r_scalar(const uint64_t *v) {
+  for (int k = 3; k >= 0; k--) {
+    if (v[k] < R_SCALAR_WORDS[k]) return 1;
+    if (v[k] > R_SCALAR_WORDS[k]) return 0;
+  }
+  return 0;
+}
+/* uniform in [0, r): 253-bit draws, words 4a..4a+3 for attempt a, rejected while >= r */
+static void uniform_scalar(uint64_t seed, uint64_t i, uint64_t *out) {
+  for (uint64_t a = 0;; a++) {
+    for (int j = 0; j < 4; j++) out[j] = oracle_rand_u64(seed, 2, i, 4 * a + (uint64_t)j);
+    out[3] &= (1ull << 61) - 1;
+    if (lt_r_scalar(out)) return;
+  }
+}
+/* the uneven-batch mix: 70% uniform, 10% 16-bit, 10% 0 or r - 1, 10% one value per MSM */
+static void mixed_scalar(uint64_t seed, uint64_t msm, uint64_t i, uint64_t *out) {
+  const uint64_t key = (msm << 32) | i;
+  const uint64_t sel = oracle_rand_u64(seed, 3, key, 0) % 10;
+  if (sel < 7) {
+    uniform_scalar(seed, key, out);
+  } else if (sel == 7) {
+    out[0] = oracle_rand_u64(seed, 3, key, 1) & 0xffff;
+    out[1] = out[2] = out[3] = 0;
+  } else if (sel == 8) {
+    if ((oracle_rand_u64(seed, 3, key, 2) & 1) == 0) {
+      out[0] = out[1] = out[2] = out[3] = 0;
+    } else {
+      for (int k = 0; k < 4; k++) out[k] = R_SCALAR_WORDS[k];
+      out[0] -= 1;
+    }
+  } else {
+    uniform_scalar(seed, (msm << 32) | 0xffffffffull, out);
+  }
+}
+/* kind 0: n uniform scalars of element indices 0..n-1; kind 1: the mix for MSM msm_index */
+int oracle_gen_scalars(uint64_t seed, uint64_t n, int kind, uint64_t msm_index, uint64_t *out,
+                       int threads) {
+  if (kind != 0 && kind != 1) return -1;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static)
+#endif
+  for (int64_t i = 0; i < (int64_t)n; i++) {
+    if (kind == 0) uniform_scalar(seed, (uint64_t)i, out + 4 * i);
+    else mixed_scalar(seed, msm_index, (uint64_t)i, out + 4 * i);
+  }
+  return 0;
+}

@@ -1,9 +1,10 @@
 """Extract the known-answer values that fyquah/hardcaml_zprize's own tests hold for the MSM path
 and write them to ``reference_kats.json`` beside this script.
 
-Run it in a checkout that has the reference tree at REF (default /root/reference):
+Run it with the path of a checkout of the reference tree, given as the first argument or in
+the environment variable HARDCAML_ZPRIZE_REF (there is no default):
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py REF
 
 It reads the reference's test and header files as text (nothing of the reference is executed)
 and records, with the file:line each value came from:
@@ -26,7 +27,10 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HARDCAML_ZPRIZE_REF", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: make_golden.py REF  (REF = a checkout of fyquah/hardcaml_zprize; "
+             "or set HARDCAML_ZPRIZE_REF)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 

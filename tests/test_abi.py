@@ -45,6 +45,14 @@ def test_host_scalar_generator_matches_oracle(engine, ref):
     assert vals.count(dup) >= 10
 
 
+def test_host_scalar_generator_matches_c_oracle(engine, ocpu):
+    # the reference arm of bench.py draws its scalars with the C oracle, the GPU arm with the
+    # engine: both must produce the same inputs for the same seed
+    assert np.array_equal(engine.generate_scalars(20240602, 5000), ocpu.gen_scalars(20240602, 5000))
+    assert np.array_equal(engine.generate_scalars(9, 3000, kind=1, msm_index=5),
+                          ocpu.gen_scalars(9, 3000, kind=1, msm_index=5))
+
+
 def test_length_mismatch_error(engine):
     ctx = engine.MultiScalarMultContext(None, 4)
     pts = np.zeros((4, 104), dtype=np.uint8)

@@ -60,3 +60,12 @@ def test_scalar_bits_above_253_ignored(ref, ocpu):
     k = ref.R_SCALAR - 5
     got = ref.decode_projective(ocpu.msm(records(ref, [p]), scal(ref, [k | (7 << 253)])).tobytes())
     assert got == ref.mul(p, k)
+
+
+def test_c_scalar_generator_matches_python(ref, ocpu):
+    got = ocpu.gen_scalars(77, 40, kind=0)
+    for i in range(40):
+        assert ref.from_limbs64(got[i]) == ref.uniform_scalar(77, i)
+    mix = ocpu.gen_scalars(77, 300, kind=1, msm_index=3)
+    for i in range(300):
+        assert ref.from_limbs64(mix[i]) == ref.mixed_scalar(77, 3, i)

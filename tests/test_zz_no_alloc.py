@@ -34,6 +34,35 @@ def test_noalloc_matches_existing_entry_point_twice(engine, ocpu):
         ctx.close()
 
 
+def test_noalloc_at_the_maximum_size_and_empty(engine, ocpu):
+    """n = 65536 (the largest size the array holds; the only caller of the unstaged scatter at
+    that size) against the existing entry point and the oracle, then n = 0, which must give
+    arkworks' zero (R, R, 0)."""
+    import torch
+
+    nbase = 70000
+    pts = ocpu.gen_bases(911, nbase)
+    ctx = engine.multi_scalar_mult_init(pts)
+    try:
+        n, off = 1 << 16, 4000
+        sc = engine.generate_scalars(912, n)
+        d_sc = torch.from_numpy(sc.view(np.uint8).reshape(-1)).cuda()
+        d_out = torch.zeros(144, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        ctx.mult_noalloc(n, off, d_sc.data_ptr(), d_out.data_ptr())
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy()
+        assert np.array_equal(got, ctx.mult_uneven([n], [off], sc)[0])
+        assert np.array_equal(got, ocpu.msm(pts[off:off + n], sc))
+        d_out.fill_(0xAB)
+        ctx.mult_noalloc(0, 0, d_sc.data_ptr(), d_out.data_ptr())
+        torch.cuda.synchronize()
+        zero = ocpu.msm(pts[:0], sc[:0])
+        assert np.array_equal(d_out.cpu().numpy(), zero)
+    finally:
+        ctx.close()
+
+
 def test_noalloc_rejects_sizes_over_the_maximum(engine, ocpu):
     import torch
 
