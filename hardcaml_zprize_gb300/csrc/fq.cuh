@@ -6,9 +6,9 @@
 // below 2q without a final subtraction.  Addition/subtraction reduce by 2q.  fq_canon() brings a
 // value to [0, q) for comparisons and for the ABI.
 //
-// The multiplier is operand-scanning CIOS with 64-bit wide multiply-adds: 12 + 11 limb products
-// per row (q's lowest limb is 1), 276 wide IMADs per product.  The survey's algorithmic count
-// for the roofline stays 588 32-bit IMAD per product (lo and hi halves of 12 x 12 + 12 x 12).
+// The multiplier is operand-scanning CIOS with 32 x 32 -> 64 wide multiplies: 12 + 11 limb
+// products per row (q's lowest limb is 1), 276 wide IMADs per product.  The algorithmic count for
+// the roofline stays 588 32-bit IMAD per product (lo and hi halves of 12 x 12 + 12 x 12).
 // The field is the one the reference computes in with GMP (host/msm_compute/include/
 // bls12_377_g1/bls12_377_g1.h:31-33, 90-219); the limb layout is new.
 #pragma once
@@ -118,35 +118,62 @@ __device__ __forceinline__ fq_t fq_one() {
 }
 
 // ---- a * b * 2^-384 mod q (CIOS; inputs and output in [0, 2q)) ----
-// Each limb product is one 32 x 32 -> 64 multiply-add into a 64-bit accumulator whose high word
-// is the next carry; the compiler issues these as wide IMADs.  On GB300 this form runs ~20% faster
-// than mad.lo/madc.hi carry chains, whose high halves issue at half rate.  Because q = 1 mod 2^32
-// and -q^-1 = -1 mod 2^32, the row factor is m = -t0 and m * q0 + t0 = 0 with a carry of
-// (t0 != 0), which saves one product per row.
+// Each row adds b_i * a and then m * q to the running value t, m = -t0 (q = 1 mod 2^32 and
+// -q^-1 = -1 mod 2^32, so the row factor needs no product and m * q0 + t0 = 0 with a carry of
+// (t0 != 0)).  The limb products are wide multiplies with no addend: a wide multiply whose 64-bit
+// addend is a 32-bit carry needs that carry moved into an aligned register pair with a zero high
+// half, and a carry folded in before the multiply needs an add-with-carry that the compiler puts
+// on the multiply pipe.  Instead each row sums four word vectors -- the products' low words, their
+// high words one word up, and the same two of m * q -- in four add.cc/addc.cc chains, which run on
+// the integer ALU pipe.  Per product (ncu, sm_103a): 276 wide multiplies and about 50 other
+// multiply-pipe instructions, against 276 and 336 for a 64-bit-accumulator CIOS; the two pipes
+// are then about equally busy.
+// Bound: at the start of a row t < 4q < 2^384 (so t[12] = 0) and no row sum leaves 13 words, for
+// any a < 2^383 and any b.
 __device__ __forceinline__ fq_t fq_mul(const fq_t &a, const fq_t &b) {
   const uint32_t q[FQ_LIMBS] = BLS_Q;
   uint32_t t[FQ_LIMBS + 1];
 #pragma unroll
-  for (int j = 0; j <= FQ_LIMBS; j++) t[j] = 0;
-#pragma unroll
   for (int i = 0; i < FQ_LIMBS; i++) {
-    uint64_t acc = 0;
+    const uint32_t bi = b.v[i];
+    uint32_t lo[FQ_LIMBS], hi[FQ_LIMBS];
 #pragma unroll
     for (int j = 0; j < FQ_LIMBS; j++) {
-      acc = (uint64_t)a.v[j] * b.v[i] + t[j] + (acc >> 32);
-      t[j] = (uint32_t)acc;
+      const uint64_t p = (uint64_t)a.v[j] * bi;
+      lo[j] = (uint32_t)p;
+      hi[j] = (uint32_t)(p >> 32);
     }
-    t[FQ_LIMBS] += (uint32_t)(acc >> 32);
+    if (i == 0) {
+#pragma unroll
+      for (int j = 0; j < FQ_LIMBS; j++) t[j] = lo[j];
+      t[FQ_LIMBS] = 0;
+    } else {
+      t[0] = add_cc(t[0], lo[0]);
+#pragma unroll
+      for (int j = 1; j < FQ_LIMBS; j++) t[j] = addc_cc(t[j], lo[j]);
+      t[FQ_LIMBS] = addc(0u, 0u);
+    }
+    t[1] = add_cc(t[1], hi[0]);
+#pragma unroll
+    for (int j = 2; j < FQ_LIMBS; j++) t[j] = addc_cc(t[j], hi[j - 1]);
+    t[FQ_LIMBS] = addc(t[FQ_LIMBS], hi[FQ_LIMBS - 1]);
     const uint32_t m = 0u - t[0];
-    acc = (uint64_t)(t[0] != 0u) << 32;
 #pragma unroll
     for (int j = 1; j < FQ_LIMBS; j++) {
-      acc = (uint64_t)m * q[j] + t[j] + (acc >> 32);
-      t[j - 1] = (uint32_t)acc;
+      const uint64_t p = (uint64_t)m * q[j];
+      lo[j] = (uint32_t)p;
+      hi[j] = (uint32_t)(p >> 32);
     }
-    acc = (uint64_t)t[FQ_LIMBS] + (acc >> 32);
-    t[FQ_LIMBS - 1] = (uint32_t)acc;
-    t[FQ_LIMBS] = (uint32_t)(acc >> 32);
+    add_cc(t[0], m);  // t0 + m = 0 mod 2^32 with a carry of (t0 != 0)
+#pragma unroll
+    for (int j = 1; j < FQ_LIMBS; j++) t[j] = addc_cc(t[j], lo[j]);
+    t[FQ_LIMBS] = addc(t[FQ_LIMBS], 0u);
+    t[2] = add_cc(t[2], hi[1]);
+#pragma unroll
+    for (int j = 3; j < FQ_LIMBS; j++) t[j] = addc_cc(t[j], hi[j - 1]);
+    t[FQ_LIMBS] = addc(t[FQ_LIMBS], hi[FQ_LIMBS - 1]);
+#pragma unroll
+    for (int j = 0; j < FQ_LIMBS; j++) t[j] = t[j + 1];
   }
   fq_t r;
 #pragma unroll
