@@ -10,8 +10,10 @@ step.  Inputs are synthetic and seeded; scalar and base buffers (512 MB + 2.4 GB
          144-byte result inside the timed region
   extra  points/s, per-step p50/p99, the uneven batch (64 MSMs of 2^10..2^20 over a shared 2^20
          base set: one pass with a shared sort replayed from a CUDA graph vs one pass per MSM),
-         the served mix (Poisson arrivals, sizes 2^12..2^22 over a 2^22 base set) and the
-         oracle port timed on the host cores.
+         the served mix (Poisson arrivals, sizes 2^12..2^22 over a 2^22 base set), the oracle
+         port timed on the host cores, the same 2^24 MSM over the plain resident form (144 B
+         per base, no tables: `plain_144B_per_base`) and the fixed-base large MSM (4 x 2^26
+         over one resident base set, batch 0 checked against the oracle: `fixed_base_4x`).
 
 `--impl reference` times the CPU port of the reference's oracle algorithm (arkworks-style
 Pippenger, oracle/cpu_msm.c) on all host cores on the same workload; the reference itself
@@ -256,6 +258,7 @@ def run_ours(args, rank, world, local):
     stats = ctx.last_pass_stats()
     ctx.set_timing(False)
     cfg = ctx.config(n)
+    ctx_info = ctx.info()
 
     # ---- e2e: host scalars through msm_mult ----
     for i in range(args.warmup):
@@ -275,7 +278,6 @@ def run_ours(args, rank, world, local):
     msm_s = t_dev / args.steps
     t_acc = stage_acc.get("accumulate", 0) * 1e-3
     entries = int(stats["entries"])  # mixed adds of one pass: its nonzero digits
-    w_tab = -(-253 // cfg["window_bits"])  # windows: fixed-base tables per base
     acc_imad = entries * C_MADD
     achieved = acc_imad / t_acc if t_acc > 0 else None
     traffic = None
@@ -293,8 +295,13 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
         "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n,
                    "l2": f"inputs larger than L2 ({n * 32 / 2**20:.0f} MB scalars, "
-                         f"{n * 144 / 2**30:.2f} GB bases"
-                         + (f", {n * w_tab * 144 / 2**30:.1f} GB fixed-base tables)" if cfg["fixed_base"] == 1 else ")"),
+                         f"{ctx_info['resident_bytes'] / 2**30:.1f} GB of resident base records: "
+                         + (f"fixed-base tables of width {ctx_info['table_bits']} "
+                            f"({ctx_info['table_windows']} records per base)"
+                            + (f" and of width {ctx_info['table2_bits']} ({ctx_info['table2_windows']} "
+                               f"records per base)" if ctx_info['table2_windows'] else "")
+                            if ctx_info['table_bits'] else "144 B per base") + "); no L2 flush needed",
+                   "resident_bytes": ctx_info["resident_bytes"],
                    "window_bits": cfg["window_bits"], "signed_digits": cfg["signed_digits"] == 1,
                    "seg_len": cfg["seg_len"], "red_len_log2": cfg["red_len_log2"],
                    "fixed_base_tables": cfg["fixed_base"] == 1},
@@ -313,8 +320,12 @@ def run_ours(args, rank, world, local):
                            "(msm_measure_int_peaks); algorithmic count 588 IMAD per 12-limb product",
             "peak_mad_lo_hi_pairs": peaks["mad_lo_hi"] / 1e12, "peak_mad_hi": peaks["mad_hi"] / 1e12,
             "frac_vs_lo_hi_pairs": (achieved / peaks["mad_lo_hi"]) if achieved else None,
-            "msm_achieved": algorithmic_imad(n) / msm_s / 1e12,
-            "msm_frac": algorithmic_imad(n) / msm_s / peak_imad,
+            # A(N) counts a windowed signed Pippenger (c in 10..16); the pass runs on fixed-base
+            # tables and does less work than that, so this is an effective rate, not a roofline
+            "effective_vs_windowed_A_N": {
+                "achieved_tera": algorithmic_imad(n) / msm_s / 1e12,
+                "frac_of_peak": algorithmic_imad(n) / msm_s / peak_imad,
+                "A_N_imad": algorithmic_imad(n)},
             # the same kernel against the copy bandwidth: how far it is from being memory-bound
             "hbm": hbm_view(entries * 148 / t_acc if t_acc > 0 else None),
         },
@@ -339,17 +350,84 @@ def run_ours(args, rank, world, local):
     if not args.skip_served and rank == 0:
         line["served"] = bench_served(args, eng, ctx, n)
     # ---- CPU baseline on the host cores, plus a bit-exact check of the GPU result ----
+    out_cpu = None
+    last_sc = host_sc[(args.steps - 1) % len(host_sc)]
     if not args.skip_cpu and rank == 0:
         cores = os.cpu_count() or 1
-        t_cpu, out_cpu = cpu_msm_time(pts, host_sc[(args.steps - 1) % len(host_sc)], cores)
+        t_cpu, out_cpu = cpu_msm_time(pts, last_sc, cores)
         line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "MSM/s", "cores": cores, "kind": "port",
                                 "sample": f"one full MSM of 2^{args.log2n} points (oracle/cpu_msm.c, "
                                           f"arkworks-0.3-style Pippenger, OpenMP over windows)"}
         line["parity_vs_cpu"] = bool(np.array_equal(last[0], out_cpu))
         line["speedup_vs_cpu"] = {"value": value * t_cpu, "e2e": e2e * t_cpu}
     ctx.close()
+    # ---- the same MSM on the plain resident form: 144 B per base, no tables ----
+    if not args.skip_plain_form and rank == 0:
+        line["plain_144B_per_base"] = bench_plain_form(args, eng, torch, dev, pts, dev_sc, last_sc,
+                                                       out_cpu, peak_imad, local)
+    del pts
+    # ---- fixed-base large MSM: 4 x 2^26 over one resident base set ----
+    if not args.skip_large and rank == 0:
+        line["fixed_base_4x"] = fixed_base_large(args, eng, peaks, local, 26, check=not args.skip_cpu)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def bench_plain_form(args, eng, torch, dev, pts, dev_sc, last_sc, out_cpu, peak_imad, local):
+    """One MSM per step over a context without fixed-base tables (MSM_FIXED_BASE=0): the
+    resident form is one 144-byte precomputed record per base and the pass is a windowed signed
+    Pippenger, as in the reference's one-record-per-point layout."""
+    n = pts.shape[0]
+    prev = os.environ.get("MSM_FIXED_BASE")
+    os.environ["MSM_FIXED_BASE"] = "0"
+    try:
+        ctx = eng.multi_scalar_mult_init(pts)
+    finally:
+        if prev is None:
+            os.environ.pop("MSM_FIXED_BASE", None)
+        else:
+            os.environ["MSM_FIXED_BASE"] = prev
+    try:
+        info = ctx.info()
+        cfg = ctx.config(n)
+        for i in range(args.warmup):
+            ctx.mult_device([n], [0], dev_sc[i % len(dev_sc)].data_ptr())
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            for i in range(args.steps):
+                ctx.mult_device([n], [0], dev_sc[i % len(dev_sc)].data_ptr())
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+        ctx.set_timing(True)
+        stages = {}
+        reps = max(2, min(args.steps, 5))
+        for i in range(reps):
+            ctx.mult_device([n], [0], dev_sc[i % len(dev_sc)].data_ptr())
+            for k, v in ctx.last_timings().items():
+                stages[k] = stages.get(k, 0.0) + v / reps
+        stats = ctx.last_pass_stats()
+        ctx.set_timing(False)
+        got = ctx.mult(last_sc)[0]
+        t_acc = stages.get("accumulate", 0) * 1e-3
+        acc_imad = int(stats["entries"]) * C_MADD
+        return {
+            "workload": f"plain single MSM, N=2^{args.log2n}, windowed signed digits over 144 B records",
+            "resident_bytes": info["resident_bytes"], "window_bits": cfg["window_bits"],
+            "value": args.steps / t, "unit": "MSM/s", "ms_per_step": 1e3 * t / args.steps,
+            "stages_ms": stages, "pass_stats": stats,
+            "roofline": {"bound": "imad", "kernel": "k_accumulate",
+                         "achieved": acc_imad / t_acc / 1e12 if t_acc else None,
+                         "peak": peak_imad / 1e12, "unit": "TIMAD/s",
+                         "frac": acc_imad / t_acc / peak_imad if t_acc else None,
+                         "algorithmic_imad_per_launch": acc_imad},
+            "windowed_A_N": {"achieved_tera": algorithmic_imad(n) / (t / args.steps) / 1e12,
+                             "frac_of_peak": algorithmic_imad(n) / (t / args.steps) / peak_imad},
+            "parity_vs_cpu": None if out_cpu is None else bool(np.array_equal(got, out_cpu)),
+            "clocks": clk.summary(),
+        }
+    finally:
+        ctx.close()
 
 
 def add_mod_r(a: np.ndarray, b: np.ndarray, r: np.ndarray) -> np.ndarray:
@@ -380,70 +458,152 @@ def add_mod_r(a: np.ndarray, b: np.ndarray, r: np.ndarray) -> np.ndarray:
     return out
 
 
-def run_fixed_base_large(args, rank, world, local):
-    """Fixed-base large MSM: 2^26 bases loaded once, then 4 independent seeded scalar vectors of
-    2^26 uniform scalars back to back (the shape of the reference's 4 x 2^26 benchmark).  Parity
-    at this size rests on size-independent properties: the fixed-base result equals the windowed
-    result (a different bucket layout and window combine), and MSM(s0) + MSM(s1) equals
-    MSM((s0 + s1) mod r)."""
-    import hardcaml_zprize_gb300 as eng
-    from hardcaml_zprize_gb300 import build
+def fixed_base_large(args, eng, peaks, local, log2n, check=True):
+    """Fixed-base large MSM: 2^log2n bases loaded once, then 4 independent seeded scalar vectors of
+    2^log2n uniform scalars back to back (the shape of the reference's 4 x 2^26 benchmark,
+    zprize/msm_pippenger/README.md:287-331).  Batch 0 is checked against the oracle on the host
+    cores (about a minute at 2^26); the others by size-independent properties: the fixed-base
+    result equals the windowed result (another bucket layout and window combine), and
+    MSM(s0) + MSM(s1) equals MSM((s0 + s1) mod r)."""
     from oracle import bls12_377 as ref
-    build.build()
-    n = 1 << args.log2n
-    os.environ["MSM_DEVICE"] = str(local)
-    peaks = eng.measure_int_peaks()
+    n = 1 << log2n
     t0 = time.perf_counter()
     pts = eng.generate_bases(args.seed, n)
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
     ctx = eng.multi_scalar_mult_init(pts)
     t_init = time.perf_counter() - t0
-    del pts
     batches = 4
     sc = np.concatenate([eng.generate_scalars(args.seed + 1 + b, n) for b in range(batches)])
-    cfg = ctx.config(n)
-    ctx.mult(sc[:n])  # warm-up
-    t0 = time.perf_counter()
-    out = ctx.mult(sc)  # 4 MSMs, one pass each, next batch's scalars uploaded during the current pass
-    t_all = time.perf_counter() - t0
-    ctx.set_timing(True)
-    ctx.mult(sc[:n])
-    stages = ctx.last_timings()
-    entries = int(ctx.last_pass_stats()["entries"])  # mixed adds of one MSM's pass
-    ctx.set_timing(False)
-    # parity by properties
-    windowed = ctx.mult(sc[:n], fixed_base=2)[0]
-    s2 = add_mod_r(sc[:n], sc[n:2 * n], np.array(ref.limbs64(ref.R_SCALAR, 4), dtype=np.uint64))
-    out2 = ctx.mult(s2)[0]
+    try:
+        cfg = ctx.config(n)
+        info = ctx.info()
+        ctx.mult(sc[:n])  # warm-up
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            out = ctx.mult(sc)  # 4 MSMs, one pass each; the next scalars go up during a pass
+            t_all = time.perf_counter() - t0
+        ctx.set_timing(True)
+        ctx.mult(sc[:n])
+        stages = ctx.last_timings()
+        stats = ctx.last_pass_stats()
+        ctx.set_timing(False)
+        entries = int(stats["entries"])
+        windowed = ctx.mult(sc[:n], fixed_base=2)[0]
+        s2 = add_mod_r(sc[:n], sc[n:2 * n], np.array(ref.limbs64(ref.R_SCALAR, 4), dtype=np.uint64))
+        out2 = ctx.mult(s2)[0]
+    finally:
+        ctx.close()
     lin = ref.add(ref.decode_projective(out[0].tobytes()), ref.decode_projective(out[1].tobytes())) == \
         ref.decode_projective(out2.tobytes())
-    ctx.close()
+    parity = {"fixed_base_equals_windowed": bool(np.array_equal(out[0], windowed)),
+              "linearity": bool(lin)}
+    if check:
+        t0 = time.perf_counter()
+        _, want = cpu_msm_time(pts, sc[:n], os.cpu_count() or 1)
+        parity["batch0_vs_cpu"] = bool(np.array_equal(out[0], want))
+        parity["cpu_s"] = time.perf_counter() - t0
     t_acc = stages.get("accumulate", 0) * 1e-3
-    value = batches / t_all
-    line = {
-        "metric": "msm_per_s", "value": value, "unit": "MSM/s", "n_gpus": world, "steps": batches,
-        "warmup": 1, "ms_per_step": 1e3 * t_all / batches, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
-        "config": {"workload": f"fixed-base large MSM, BLS12-377 G1, 2^{args.log2n} resident bases, "
-                               f"4 scalar vectors back to back", "n": n,
-                   "window_bits": cfg["window_bits"], "fixed_base_tables": cfg["fixed_base"] == 1},
-        "e2e": {"value": value, "unit": "MSM/s", "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": 144},
-        "per_batch_latency_ms": 1e3 * t_all / batches,
-        "stages_ms": stages,
+    return {
+        "workload": f"fixed-base large MSM, BLS12-377 G1, 2^{log2n} resident bases, "
+                    f"{batches} scalar vectors back to back, host scalars (msm_mult)",
+        "n": n, "batches": batches, "msm_per_s": batches / t_all,
+        "per_batch_latency_ms": 1e3 * t_all / batches, "total_s": t_all,
+        "window_bits": cfg["window_bits"], "resident_bytes": info["resident_bytes"],
+        "h2d_bytes_per_batch": n * 32, "d2h_bytes_per_batch": 144,
+        "stages_ms": stages, "pass_stats": stats,
         "hbm_gbs_base_and_scalar_streams": (entries * 148 + n * 32) / t_acc / 1e9 if t_acc else None,
-        "imad": {"achieved_tera": entries * C_MADD / t_acc / 1e12 if t_acc else None,
+        "imad": {"kernel": "k_accumulate", "achieved_tera": entries * C_MADD / t_acc / 1e12 if t_acc else None,
                  "peak_mad_lo_tera": peaks["mad_lo"] / 1e12,
                  "frac": (entries * C_MADD / t_acc / peaks["mad_lo"]) if t_acc else None,
                  "entries_per_msm": entries},
-        "parity": {"fixed_base_equals_windowed": bool(np.array_equal(out[0], windowed)),
-                   "linearity": bool(lin)},
+        "parity": parity, "clocks": clk.summary(),
         "setup_s": {"generate_bases": t_gen, "msm_init_with_tables": t_init},
-        "reference_fpga": {"value": 4 / 20.336, "unit": "MSM/s",
+        "reference_fpga": {"total_s": 20.336, "msm_per_s": 4 / 20.336,
                            "source": "reference README: 4 x 2^26 in 20.336 s on AWS F1 (not run here)"},
     }
+
+
+def run_fixed_base_large(args, rank, world, local):
+    """`--workload fixed_base_4x`: the fixed-base block alone, as its own line."""
+    import hardcaml_zprize_gb300 as eng
+    from hardcaml_zprize_gb300 import build
+    build.build()
+    os.environ["MSM_DEVICE"] = str(local)
+    if rank != 0:
+        return
+    peaks = eng.measure_int_peaks()
+    res = fixed_base_large(args, eng, peaks, local, args.log2n, check=not args.skip_cpu)
+    line = {
+        "metric": "msm_per_s", "value": res["msm_per_s"], "unit": "MSM/s", "n_gpus": world,
+        "steps": res["batches"], "warmup": 1, "ms_per_step": res["per_batch_latency_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
+        "config": {"workload": res["workload"], "n": res["n"], "window_bits": res["window_bits"]},
+        "e2e": {"value": res["msm_per_s"], "unit": "MSM/s", "h2d_bytes_per_step": res["n"] * 32,
+                "d2h_bytes_per_step": 144},
+        "clocks": res["clocks"], "fixed_base_4x": res,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_sharded(args, rank, world, local):
+    """`--workload sharded`: one MSM of 2^log2n points split into contiguous base slices, one per
+    rank (each rank keeps only its slice resident), one all-gather of the 144-byte partial points
+    (NCCL under torchrun, nothing at one rank) and an engine MSM with scalars 1 that adds them.
+    Total work is fixed as ranks are added (strong scaling)."""
+    import hardcaml_zprize_gb300 as eng
+    from hardcaml_zprize_gb300 import build, shard
+    build.build()
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    os.environ["MSM_DEVICE"] = str(local)
+    n = 1 << args.log2n
+    lo, hi = shard.partition(n, world)[rank]
+    pts = eng.generate_bases(args.seed, hi - lo, first=lo)
+    ctx = eng.multi_scalar_mult_init(pts)
+    sc = eng.generate_scalars(args.seed + 1, n)
+    d_sc = torch.from_numpy(sc[lo:hi].view(np.uint8).reshape(-1)).to(dev)
+    torch.cuda.synchronize()
+
+    def partial(a, b):
+        return ctx.mult_device([b - a], [0], d_sc.data_ptr())[0]
+
+    def step():
+        if world == 1:
+            return shard.combine_on_gpu([partial(lo, hi)])
+        return shard.sharded_msm(n, rank, world, partial, shard.combine_on_gpu)
+
+    for _ in range(args.warmup):
+        out = step()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = step()
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+    barrier(world)
+    t = max_over_ranks(t, world)
+    parity = None
+    if rank == 0 and not args.skip_cpu:
+        from oracle import cpu as ocpu
+        parity = bool(np.array_equal(out, ocpu.msm(eng.generate_bases(args.seed, n), sc)))
+    ctx.close()
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps({
+            "metric": "msm_per_s", "value": args.steps / t, "unit": "MSM/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
+            "config": {"workload": f"one MSM of N=2^{args.log2n} sharded over {world} rank(s) by "
+                                   f"base slices, one all-gather of partial points", "n": n,
+                       "bases_per_rank": hi - lo},
+            "e2e": {"value": args.steps / t, "unit": "MSM/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 144 * world},
+            "parity_vs_cpu": parity, "clocks": clk.summary()}), flush=True)
 
 
 def uneven_mix(seed: int, gen_scalars, m: int = 64, nbase: int = 1 << 20):
@@ -490,6 +650,23 @@ def bench_batched(args, eng, ctx, torch, dev):
             ctx.mult_uneven(sizes, offs, sc, **opts)
         te = (time.perf_counter() - t0) / reps
         res[name]["e2e_msm_per_s"] = m / te
+    # the autotuner on this mix (untimed), then the tuned one-pass form
+    if args.tune_budget_ms > 0:
+        tr = ctx.tune_uneven(sizes, offs, sc, budget_ms=args.tune_budget_ms)
+        topts = {k: v for k, v in tr["opts"].items() if k != "mode"}
+        for _ in range(max(args.warmup, 2)):
+            outs["batched_tuned"] = ctx.mult_device(sizes, offs, dsc.data_ptr(), mode=2, use_graph=1, **topts)
+        reps = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            outs["batched_tuned"] = ctx.mult_device(sizes, offs, dsc.data_ptr(), mode=2, use_graph=1, **topts)
+        t = (time.perf_counter() - t0) / reps
+        res["batched_tuned"] = {"msm_per_s": m / t, "points_per_s": sum(sizes) / t, "ms_per_batch": 1e3 * t,
+                                "tuner": {"untuned_pass_ms": tr["untuned_ms"], "tuned_pass_ms": tr["tuned_ms"],
+                                          "passes_measured": tr["passes_measured"], "pass_options": topts,
+                                          "forms_by_log2_size": {str(k): v for k, v in tr["forms"].items()}},
+                                "identical_results": bool(np.array_equal(outs["batched_tuned"], outs["plain"]))}
+        res["ratio_batched_tuned_over_plain"] = res["batched_tuned"]["msm_per_s"] / res["plain"]["msm_per_s"]
     # the same 64 MSMs as served requests arriving back to back (continuous batching)
     srv = eng.MsmServer(ctx, hbm_budget_bytes=args.served_budget_gb << 30, max_inflight=2)
     first = np.concatenate([[0], np.cumsum(sizes)])
@@ -530,12 +707,12 @@ def bench_served(args, eng, ctx, n):
     plain_rate = m / t_plain
     out = {"plain_msm_per_s": plain_rate, "requests": m, "sizes": "log-uniform 2^12..2^22",
            "base_set": nbase, "rates": []}
-    for mult in args.served_load:
+    for mult, inflight in [(a, b) for a in args.served_load for b in args.served_inflight]:
         lam = plain_rate * mult
         gaps = rng.exponential(1.0 / lam, m)
-        srv = eng.MsmServer(ctx, hbm_budget_bytes=args.served_budget_gb << 30, max_inflight=2)
-        # untimed warm-up: the two largest requests, so both slots hold their workspaces
-        big = sorted(range(m), key=lambda j: -sizes[j])[:2]
+        srv = eng.MsmServer(ctx, hbm_budget_bytes=args.served_budget_gb << 30, max_inflight=inflight)
+        # untimed warm-up: the largest requests, so every slot holds its workspace
+        big = sorted(range(m), key=lambda j: -sizes[j])[:inflight]
         for rid in [srv.submit(reqs[j], offs[j]) for j in big]:
             srv.poll(rid, wait_ms=600000)
         p_before = srv.stats()["passes"]
@@ -556,7 +733,8 @@ def bench_served(args, eng, ctx, n):
         t = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        out["rates"].append({"offered_per_s": lam, "msm_per_s": m / t, "p50_ms": percentile(lats, 50),
+        out["rates"].append({"offered_per_s": lam, "load_vs_plain": mult, "max_inflight": inflight,
+                             "msm_per_s": m / t, "p50_ms": percentile(lats, 50),
                              "p99_ms": percentile(lats, 99), "passes": st["passes"] - p_before,
                              "inflight_peak": st["inflight_peak"], "same_as_alone": exact})
     return out
@@ -573,12 +751,20 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-plain-form", action="store_true",
+                    help="skip the 144 B-per-base (no tables) form of the headline MSM")
+    ap.add_argument("--skip-large", action="store_true", help="skip the 4 x 2^26 fixed-base block")
+    ap.add_argument("--tune-budget-ms", type=int, default=15000,
+                    help="time the batch autotuner may spend on the uneven mix (0: skip it)")
     ap.add_argument("--served-requests", type=int, default=48)
     ap.add_argument("--served-load", type=float, nargs="*", default=[0.5, 1.5])
     ap.add_argument("--served-budget-gb", type=int, default=16)
-    ap.add_argument("--workload", default="plain", choices=["plain", "fixed_base_4x"],
+    ap.add_argument("--served-inflight", type=int, nargs="*", default=[2, 4],
+                    help="server slots (passes in flight) to sweep at each offered load")
+    ap.add_argument("--workload", default="plain", choices=["plain", "fixed_base_4x", "sharded"],
                     help="plain: the default single-MSM line; fixed_base_4x: 4 MSMs over one "
-                         "resident base set (use with --log2n 26)")
+                         "resident base set (use with --log2n 26); sharded: one MSM split over "
+                         "the ranks by base slices")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # timed numbers always follow at least 3 warm-up steps
     rank, world, local = dist_setup()
@@ -586,6 +772,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "fixed_base_4x":
         run_fixed_base_large(args, rank, world, local)
+    elif args.workload == "sharded":
+        run_sharded(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

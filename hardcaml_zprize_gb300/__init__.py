@@ -32,7 +32,7 @@ SCALAR_BYTES = 32
 # every symbol include/msm_gb300.h declares
 EXPORTED = [
     "msm_init", "msm_mult", "msm_last_error", "msm_free", "msm_mult_ex", "msm_mult_uneven",
-    "msm_mult_device", "msm_get_config", "msm_context_info", "msm_tune", "msm_set_timing", "msm_last_timings",
+    "msm_mult_device", "msm_get_config", "msm_context_info", "msm_tune_uneven", "msm_tuned_form", "msm_tune", "msm_set_timing", "msm_last_timings",
     "msm_last_pass_stats", "msm_server_create", "msm_server_submit", "msm_server_poll",
     "msm_server_stats", "msm_server_destroy", "msm_generate_bases", "msm_generate_scalars",
     "msm_measure_imad_peak", "msm_device_info", "msm_field_selftest", "msm_measure_madd_rate",
@@ -87,6 +87,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "msm_mult_device": (ctypes.c_int, [P, P, U64, P, P, P, ctypes.POINTER(MsmOptions)]),
         "msm_get_config": (ctypes.c_int, [P, U64, ctypes.POINTER(MsmOptions)]),
         "msm_context_info": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_uint64), I32]),
+        "msm_tune_uneven": (ctypes.c_int, [P, U64, P, P, P, I32, ctypes.POINTER(MsmOptions),
+                                           ctypes.POINTER(ctypes.c_double)]),
+        "msm_tuned_form": (ctypes.c_int, [P, U64, I32, ctypes.POINTER(MsmOptions)]),
         "msm_tune": (ctypes.c_int, [P, U64, I32, ctypes.POINTER(MsmOptions)]),
         "msm_set_timing": (ctypes.c_int, [P, I32]),
         "msm_last_timings": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double), I32]),
@@ -229,6 +232,34 @@ class MultiScalarMultContext:
         o = MsmOptions()
         _check(load_library().msm_tune(self.handle, n, budget_ms, ctypes.byref(o)), "msm_tune")
         return {f: getattr(o, f) for f, _ in MsmOptions._fields_}
+
+    def tune_uneven(self, sizes: Sequence[int], offsets: Sequence[int], scalars,
+                    budget_ms: int = 0) -> dict:
+        """Tune the one-pass form on this batch (msm_tune_uneven).  Returns the pass-level options
+        to pass back with the same mix (``opts``), the untuned and tuned pass times (ms) and the
+        per-size-class forms now used in shared passes."""
+        sc = as_scalars(scalars)
+        sz = np.ascontiguousarray(sizes, dtype=np.uint64)
+        of = np.ascontiguousarray(offsets, dtype=np.uint64)
+        if sc.shape[0] != int(sz.sum()):
+            raise ValueError("length mismatch")
+        o = MsmOptions()
+        rep = (ctypes.c_double * 3)()
+        _check(load_library().msm_tune_uneven(self.handle, len(sz), _ptr(sz), _ptr(of), _ptr(sc),
+                                              budget_ms, ctypes.byref(o), rep), "msm_tune_uneven")
+        opts = {f: getattr(o, f) for f, _ in MsmOptions._fields_ if getattr(o, f)}
+        classes = sorted({(max(int(x), 1) - 1).bit_length() for x in sz})  # ceil(log2 n)
+        forms = {c: self.tuned_form(1 << c, shared_pass=True) for c in classes}
+        return {"opts": opts, "untuned_ms": rep[0], "tuned_ms": rep[1], "passes_measured": int(rep[2]),
+                "forms": forms}
+
+    def tuned_form(self, n: int, shared_pass: bool = False) -> dict:
+        """Window width, digit signs and the bases read (0 plain records, 1 main tables,
+        2 width-16 tables) for an MSM of n points, alone or in a shared pass."""
+        o = MsmOptions()
+        _check(load_library().msm_tuned_form(self.handle, n, 1 if shared_pass else 0, ctypes.byref(o)),
+               "msm_tuned_form")
+        return {"window_bits": o.window_bits, "signed": o.signed_digits == 1, "bases": o.fixed_base}
 
     def set_timing(self, on: bool):
         _check(load_library().msm_set_timing(self.handle, 1 if on else 0), "msm_set_timing")

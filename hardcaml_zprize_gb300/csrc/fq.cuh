@@ -221,6 +221,30 @@ __device__ __forceinline__ fq_t fq_sub(const fq_t &a, const fq_t &b) {
   return r;
 }
 
+// Unreduced forms for operands that only feed products: for a, b < 2q, a + b and a - b + 2q are
+// below 4q, and a product of two values below 4q is again below 2q (16q < 2^384).
+__device__ __forceinline__ fq_t fq_add_lazy(const fq_t &a, const fq_t &b) {
+  fq_t r;
+  r.v[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) r.v[j] = addc_cc(a.v[j], b.v[j]);
+  r.v[FQ_LIMBS - 1] = addc(a.v[FQ_LIMBS - 1], b.v[FQ_LIMBS - 1]);
+  return r;
+}
+__device__ __forceinline__ fq_t fq_sub_lazy(const fq_t &a, const fq_t &b) {
+  const uint32_t q2[FQ_LIMBS] = BLS_Q2;
+  uint32_t d[FQ_LIMBS];
+  d[0] = add_cc(a.v[0], q2[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS; j++) d[j] = addc_cc(a.v[j], q2[j]);
+  fq_t r;
+  r.v[0] = sub_cc(d[0], b.v[0]);
+#pragma unroll
+  for (int j = 1; j < FQ_LIMBS - 1; j++) r.v[j] = subc_cc(d[j], b.v[j]);
+  r.v[FQ_LIMBS - 1] = subc(d[FQ_LIMBS - 1], b.v[FQ_LIMBS - 1]);
+  return r;
+}
+
 __device__ __forceinline__ fq_t fq_neg(const fq_t &a) { return fq_sub(fq_zero(), a); }
 
 __device__ __forceinline__ fq_t fq_dbl(const fq_t &a) { return fq_add(a, a); }

@@ -527,6 +527,10 @@ struct Ctx {
   double last_ms[MSM_NUM_STAGES] = {0};
   uint64_t last_stats[5] = {0};  // tasks, heavy buckets, sorted entries, buckets, kernels
   std::map<uint32_t, Cfg> tuned;  // by log2 size class
+  // forms tuned for MSMs that share a pass with others (msm_tune_uneven), by log2 size class;
+  // a shared pass overlaps the serial tails of its MSMs, so the best form can differ from the
+  // best for one MSM alone
+  std::map<uint32_t, Cfg> tuned_batch;
   ~Ctx() {
     if (stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -667,10 +671,13 @@ int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
   return 0;
 }
 
-Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt) {
+Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt, bool shared_pass = false) {
   Cfg cfg = heuristic_cfg(n);
-  auto it = cx->tuned.find(log2_ceil(std::max<uint64_t>(n, 1)));
-  const bool tuned = it != cx->tuned.end();
+  const uint32_t cls = log2_ceil(std::max<uint64_t>(n, 1));
+  const std::map<uint32_t, Cfg> &tmap =
+      shared_pass && cx->tuned_batch.count(cls) ? cx->tuned_batch : cx->tuned;
+  auto it = tmap.find(cls);
+  const bool tuned = it != tmap.end();
   if (tuned) cfg = it->second;
   const bool forced_c = opt && opt->window_bits > 0;
   if (opt) {
@@ -766,9 +773,9 @@ int run_msms(Ctx *cx, g1_projective_t *out, const std::vector<uint64_t> &sizes,
     uint64_t maxn = 0;
     for (size_t j = 0; j < m; j++) maxn = std::max(maxn, sizes[j]);
     for (size_t j = 0; j < m; j++) {
-      specs[j] = {sizes[j], offs[j], first[j], resolve_cfg(cx, sizes[j], opt)};
-      specs[j].cfg.seg_len = resolve_cfg(cx, maxn, opt).seg_len;
-      specs[j].cfg.red_log2 = resolve_cfg(cx, maxn, opt).red_log2;
+      specs[j] = {sizes[j], offs[j], first[j], resolve_cfg(cx, sizes[j], opt, m > 1)};
+      specs[j].cfg.seg_len = resolve_cfg(cx, maxn, opt, m > 1).seg_len;
+      specs[j].cfg.red_log2 = resolve_cfg(cx, maxn, opt, m > 1).red_log2;
       set_tables(cx, specs[j]);
     }
     if (m > 1 && !(opt && opt->seg_len > 0)) {
@@ -874,7 +881,10 @@ void load_tune_cache(Ctx *cx) {
   char line[256];
   while (fgets(line, sizeof(line), f)) {
     fx = 0;  // a seventh field (1: the fixed-base form) is optional
-    if (sscanf(line, "%u %u %u %u %u %lf %u", &lg, &c, &sg, &seg, &red, &ms, &fx) < 6) continue;
+    // lines starting with "b" hold forms tuned for MSMs sharing a pass (msm_tune_uneven)
+    const bool shared = line[0] == 'b';
+    if (sscanf(line + (shared ? 1 : 0), "%u %u %u %u %u %lf %u", &lg, &c, &sg, &seg, &red, &ms, &fx) < 6)
+      continue;
     if (lg > 40 || c < 4 || c > 24 || seg == 0 || seg > 4096 || red > 12) continue;
     Cfg cf;
     cf.c = c;
@@ -882,7 +892,7 @@ void load_tune_cache(Ctx *cx) {
     cf.seg_len = seg;
     cf.red_log2 = red;
     cf.fixed = fx <= 2 ? fx : 0;
-    cx->tuned[lg] = cf;
+    (shared ? cx->tuned_batch : cx->tuned)[lg] = cf;
   }
   fclose(f);
 }
@@ -1243,9 +1253,11 @@ void Server::loop() {
         std::vector<JobSpec> specs(batch.size());
         uint64_t maxn = 0, first = 0;
         for (auto &r : batch) maxn = std::max(maxn, r->n);
-        const Cfg big = resolve_cfg(cx, maxn, nullptr);
+        const bool shared = batch.size() > 1;
+        const Cfg big = resolve_cfg(cx, maxn, nullptr, shared);
         for (size_t j = 0; j < batch.size(); j++) {
-          specs[j] = {batch[j]->n, batch[j]->base_off, first, resolve_cfg(cx, batch[j]->n, nullptr)};
+          specs[j] = {batch[j]->n, batch[j]->base_off, first,
+                      resolve_cfg(cx, batch[j]->n, nullptr, shared)};
           specs[j].cfg.seg_len = big.seg_len;
           specs[j].cfg.red_log2 = big.red_log2;
           set_tables(cx, specs[j]);
@@ -1559,6 +1571,194 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
     best_out->mode = 1;
     best_out->fixed_base = best.fixed ? 1 : 2;
   }
+  return 0;
+}
+
+int msm_tune_uneven(void *context, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const biginteger256_t *scalars, int32_t budget_ms,
+                    msm_options_t *best_out, double *report) {
+  g_err = 0;
+  auto *cx = (Ctx *)context;
+  if (!cx || num_msms == 0 || !sizes || !base_offsets || !scalars)
+    return fail(ERR_ARG, "msm_tune_uneven: null argument");
+  const size_t m = num_msms;
+  std::vector<uint64_t> first(m + 1, 0);
+  for (size_t j = 0; j < m; j++) {
+    if (base_offsets[j] > cx->npoints || sizes[j] > cx->npoints - base_offsets[j])
+      return fail(ERR_ARG, "msm_tune_uneven: MSM %zu outside the resident bases", j);
+    first[j + 1] = first[j] + sizes[j];
+  }
+  if (budget_ms <= 0) budget_ms = 20000;
+  std::lock_guard<std::mutex> lk(cx->mu);
+  if (cudaSetDevice(cx->device) != cudaSuccess) return fail(ERR_DEVICE, "cudaSetDevice failed");
+  DevBuf dsc;
+  CK(dsc.ensure(std::max<uint64_t>(first[m], 1) * 32));
+  if (first[m]) CK(cudaMemcpy(dsc.p, scalars, first[m] * 32, cudaMemcpyHostToDevice));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const auto t_start = std::chrono::steady_clock::now();
+  auto spent_ms = [&] {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start)
+        .count();
+  };
+  // one pass of the whole mix with the forms in `form` (by size class) and the pass-level run
+  // length (0: the automatic rule) and level-1 reduction run (0: automatic); best of 2 timed runs
+  auto time_pass = [&](const std::map<uint32_t, Cfg> &form, uint32_t seg, uint32_t red) -> double {
+    std::vector<JobSpec> specs(m);
+    for (size_t j = 0; j < m; j++) {
+      specs[j] = {sizes[j], base_offsets[j], first[j], form.at(log2_ceil(std::max<uint64_t>(sizes[j], 1)))};
+      specs[j].cfg.red_log2 = red;
+      set_tables(cx, specs[j]);
+    }
+    const uint32_t s2 = seg ? seg : pass_seg_len(specs);
+    for (JobSpec &sp : specs) sp.cfg.seg_len = s2;
+    Plan pl;
+    if (build_plan(specs, pl)) return 1e300;
+    double t = 1e300;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, cx->stream);
+      if (enqueue_pass(cx, cx->ws, pl, dsc.p, cx->stream, false, false, 0)) return 1e300;
+      cudaEventRecord(e1, cx->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return 1e300;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) t = std::min(t, (double)ms);
+    }
+    uint32_t cnt[CNT_WORDS];
+    if (cudaMemcpy(cnt, cx->ws.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cnt[CNT_ERROR])
+      return 1e300;
+    return t;
+  };
+  // size classes, largest total points first, and their starting forms: what a shared pass
+  // would use untuned (the cost model's choice at the class's largest size)
+  std::map<uint32_t, uint64_t> pts_of, max_of;
+  for (size_t j = 0; j < m; j++) {
+    const uint32_t cls = log2_ceil(std::max<uint64_t>(sizes[j], 1));
+    pts_of[cls] += sizes[j];
+    max_of[cls] = std::max(max_of[cls], sizes[j]);
+  }
+  std::map<uint32_t, Cfg> form;
+  for (auto &kv : max_of) form[kv.first] = resolve_cfg(cx, kv.second, nullptr, false);
+  std::vector<uint32_t> order;
+  for (auto &kv : pts_of) order.push_back(kv.first);
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return pts_of[a] > pts_of[b]; });
+  const double untuned = time_pass(form, 0, 0);
+  double best = untuned;
+  int measured = 1;
+  // coordinate descent over the classes: windowed signed c = 10..16, windowed unsigned at the
+  // best windowed width, and each table set of the context
+  for (uint32_t cls : order) {
+    if (spent_ms() > budget_ms) break;
+    std::vector<Cfg> cands;
+    for (uint32_t c = 10; c <= 16; c++) {
+      Cfg cf;
+      cf.c = c;
+      cf.signed_digits = 1;
+      cf.fixed = 0;
+      cands.push_back(cf);
+    }
+    for (uint32_t which = 1; which <= 2; which++) {
+      const uint32_t tc = which == 1 ? cx->fb_c : cx->fb2_c;
+      if (!tc) continue;
+      Cfg cf;
+      cf.c = tc;
+      cf.signed_digits = 1;
+      cf.fixed = which;
+      cands.push_back(cf);
+    }
+    uint32_t best_windowed_c = form[cls].fixed ? 0 : form[cls].c;
+    double best_windowed = 1e300;
+    for (size_t k = 0; k <= cands.size(); k++) {
+      if (spent_ms() > budget_ms) break;
+      Cfg cf;
+      if (k < cands.size()) {
+        cf = cands[k];
+      } else {  // unsigned digits at the best windowed width
+        if (!best_windowed_c) break;
+        cf.c = std::min<uint32_t>(best_windowed_c, 16);
+        cf.signed_digits = 0;
+        cf.fixed = 0;
+      }
+      std::map<uint32_t, Cfg> trial = form;
+      trial[cls] = cf;
+      const double t = time_pass(trial, 0, 0);
+      measured++;
+      if (!cf.fixed && cf.signed_digits && t < best_windowed) {
+        best_windowed = t;
+        best_windowed_c = cf.c;
+      }
+      if (t < best) {
+        best = t;
+        form[cls] = cf;
+      }
+    }
+  }
+  // pass-level knobs: run length (how many threads share a heavy bucket) and level-1 reduction
+  uint32_t best_seg = 0, best_red = 0;
+  {
+    std::vector<JobSpec> specs(m);
+    for (size_t j = 0; j < m; j++) {
+      specs[j] = {sizes[j], base_offsets[j], first[j], form.at(log2_ceil(std::max<uint64_t>(sizes[j], 1)))};
+      set_tables(cx, specs[j]);
+    }
+    const uint32_t auto_seg = pass_seg_len(specs);
+    for (uint32_t seg : {auto_seg / 4, auto_seg / 2, auto_seg * 2, auto_seg * 4}) {
+      if (seg < 8 || seg > 4096 || spent_ms() > budget_ms) continue;
+      const double t = time_pass(form, seg, 0);
+      measured++;
+      if (t < best) {
+        best = t;
+        best_seg = seg;
+      }
+    }
+    for (uint32_t red = 2; red <= 6; red++) {
+      if (spent_ms() > budget_ms) break;
+      const double t = time_pass(form, best_seg, red);
+      measured++;
+      if (t < best) {
+        best = t;
+        best_red = red;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto &kv : form) cx->tuned_batch[kv.first] = kv.second;
+  if (const char *path = getenv("MSM_TUNE_CACHE")) {
+    if (FILE *f = fopen(path, "a")) {
+      for (auto &kv : form)
+        fprintf(f, "b %u %u %u %u %u %.4f %u\n", kv.first, kv.second.c, kv.second.signed_digits,
+                kv.second.seg_len, kv.second.red_log2, best, kv.second.fixed);
+      fclose(f);
+    }
+  }
+  if (best_out) {
+    *best_out = msm_options_t{};
+    best_out->seg_len = (int32_t)best_seg;
+    best_out->red_len_log2 = (int32_t)best_red;
+    best_out->mode = 2;
+  }
+  if (report) {
+    report[0] = untuned;
+    report[1] = best;
+    report[2] = measured;
+  }
+  return 0;
+}
+
+int msm_tuned_form(void *context, uint64_t npoints, int32_t shared_pass, msm_options_t *out) {
+  auto *cx = (Ctx *)context;
+  if (!cx || !out) return fail(ERR_ARG, "msm_tuned_form: null argument");
+  const Cfg c = resolve_cfg(cx, npoints, nullptr, shared_pass != 0);
+  *out = msm_options_t{};
+  out->window_bits = (int32_t)c.c;
+  out->signed_digits = c.signed_digits ? 1 : 2;
+  out->seg_len = (int32_t)c.seg_len;
+  out->red_len_log2 = (int32_t)c.red_log2;
+  out->fixed_base = (int32_t)c.fixed;  // 0 plain records, 1 main tables, 2 width-16 tables
+  out->mode = shared_pass ? 2 : 1;
   return 0;
 }
 

@@ -583,16 +583,20 @@ __device__ __forceinline__ fq_t staged_fq(const uint4 *sh, int part) {
   return r;
 }
 
-// te_madd with the base ((y-x)/2, (y+x)/2, d x y) read from the staging slots
+// te_madd with the base ((y-x)/2, (y+x)/2, d x y) read from the staging slots.  Sums and
+// differences that only feed products stay unreduced (below 4q; every product is again below
+// 2q), and a negative digit swaps F and G instead of negating C: with C' = -C, Z - C' = Z + C
+// and Z + C' = Z - C.  Measured in the mixed-add loop on GB300: 3.00e9 against 2.92e9 madd/s.
 __device__ __forceinline__ xyzt_t te_madd_staged(const xyzt_t &p, const uint4 *sh, bool neg) {
-  const fq_t A = fq_mul_nv(fq_sub(p.y, p.x), staged_fq(sh, neg ? 1 : 0));
-  const fq_t B = fq_mul_nv(fq_add(p.y, p.x), staged_fq(sh, neg ? 0 : 1));
-  fq_t C = fq_mul_nv(p.t, staged_fq(sh, 2));
-  C = fq_select(neg, fq_neg(C), C);
-  const fq_t E = fq_sub(B, A);
-  const fq_t H = fq_add(B, A);
-  const fq_t F = fq_sub(p.z, C);
-  const fq_t G = fq_add(p.z, C);
+  const fq_t A = fq_mul_nv(fq_sub_lazy(p.y, p.x), staged_fq(sh, neg ? 1 : 0));
+  const fq_t B = fq_mul_nv(fq_add_lazy(p.y, p.x), staged_fq(sh, neg ? 0 : 1));
+  const fq_t C = fq_mul_nv(p.t, staged_fq(sh, 2));
+  const fq_t E = fq_sub_lazy(B, A);
+  const fq_t H = fq_add_lazy(B, A);
+  const fq_t Zm = fq_sub_lazy(p.z, C);
+  const fq_t Zp = fq_add_lazy(p.z, C);
+  const fq_t F = fq_select(neg, Zp, Zm);
+  const fq_t G = fq_select(neg, Zm, Zp);
   xyzt_t r;
   r.x = fq_mul_nv(E, F);
   r.y = fq_mul_nv(G, H);

@@ -133,6 +133,26 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
  * values written (at most 6). */
 int msm_context_info(void *context, uint64_t *info, int32_t max_info);
 
+/* Tune the one-pass form of a batch of uneven MSMs on that batch itself (same arguments as
+ * msm_mult_uneven, host scalars). Per size class (log2 of the MSM size) it measures whole passes
+ * of the batch with signed windows of width 10..16, unsigned windows at the best width and each
+ * fixed-base table set of the context, by coordinate descent from the largest classes down; then
+ * the pass's run length (entries one thread accumulates before a bucket is split over more
+ * threads: the threads-per-bucket knob) and level-1 reduction run. The class forms are kept for
+ * later passes that several MSMs share (msm_mult_uneven with mode 2, server passes) and appended
+ * to MSM_TUNE_CACHE as "b ..." lines; the pass-level knobs come back in `best` (mode 2) for the
+ * caller to pass with the same mix. `report` (may be NULL) receives the untuned and tuned pass
+ * times in ms and the number of passes measured. `budget_ms` bounds the time (0: 20 s).
+ * The reference fixes its window layout in RTL (hardcaml/src/config.ml:5-21,
+ * config_utils.ml:7-49); this has no counterpart there. */
+int msm_tune_uneven(void *context, uint64_t num_msms, const uint64_t *sizes,
+                    const uint64_t *base_offsets, const biginteger256_t *scalars, int32_t budget_ms,
+                    msm_options_t *best, double *report);
+/* The form the engine uses for an MSM of `npoints`, alone (shared_pass 0) or in a pass with
+ * others (1): window_bits, signed_digits, and in fixed_base the bases it reads (here 0: the plain
+ * records, windowed; 1: the main fixed-base table set; 2: the second, width-16 set). */
+int msm_tuned_form(void *context, uint64_t npoints, int32_t shared_pass, msm_options_t *out);
+
 /* Per-stage device times (ms, CUDA events on the pipeline stream) of the last pass when timing
  * is enabled with msm_set_timing(ctx, 1). Stage order: count, scan, scatter, tasks, accumulate,
  * merge, reduce1, reduce2, reduce3, final. Returns the number of stages written. */
