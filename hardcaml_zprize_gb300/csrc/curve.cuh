@@ -199,7 +199,8 @@ static __device__ __noinline__ wpt_t w_add(const wpt_t &p, const wpt_t &q) {  //
 // inversion: u = (Z+Y)/(Z-Y), v = ts*u*Z/X, x_w = u/c_B + c_A/(3 c_B), y_w = v/c_B.
 // The identity maps to infinity; the order-two point (0, -1) maps to its Weierstrass image
 // (c_A/(3 c_B), 0) (the reference sends both x = 0 points to infinity, :393-396).
-static __device__ __noinline__ wpt_t te_to_weierstrass(const xyzt_t &p) {
+template <bool QUAD>
+__device__ __forceinline__ wpt_t te_to_weierstrass_t(const xyzt_t &p, uint32_t mask) {
   const uint32_t ts[FQ_LIMBS] = BLS_TWISTED_SCALE;
   const uint32_t icb[FQ_LIMBS] = BLS_INV_CB;
   const uint32_t ca3[FQ_LIMBS] = BLS_CA_OVER_3CB;
@@ -213,13 +214,23 @@ static __device__ __noinline__ wpt_t te_to_weierstrass(const xyzt_t &p) {
   }
   const fq_t zpy = fq_add(p.z, p.y);
   const fq_t zmy = fq_sub(p.z, p.y);
-  const fq_t inv = fq_inv_vartime(fq_mul_ool(zmy, p.x));
+  const fq_t den = fq_mul_ool(zmy, p.x);
+  const fq_t inv = QUAD ? fq_inv_quad(den, mask) : fq_inv_vartime(den);
   const fq_t u = fq_mul_ool(fq_mul_ool(zpy, p.x), inv);
   const fq_t v = fq_mul_ool(fq_mul_ool(fq_mul_ool(zpy, p.z), inv), fq_from(ts));
   r.x = fq_add(fq_mul_ool(u, fq_from(icb)), fq_from(ca3));
   r.y = fq_mul_ool(v, fq_from(icb));
   r.z = fq_one();
   return r;
+}
+
+static __device__ __noinline__ wpt_t te_to_weierstrass(const xyzt_t &p) {
+  return te_to_weierstrass_t<false>(p, 0u);
+}
+// The same map run by the four lanes of a quad that all hold p (`mask` covers them): the
+// inversion is shared between the lanes (fq_inv_quad); every lane returns the result.
+static __device__ __noinline__ wpt_t te_to_weierstrass_quad(const xyzt_t &p, uint32_t mask) {
+  return te_to_weierstrass_t<true>(p, mask);
 }
 
 // Jacobian -> affine with z in {0, 1}, all coordinates canonical in [0, q)

@@ -328,6 +328,66 @@ static __device__ __noinline__ fq_t fq_inv_vartime(const fq_t &a) {
   return fq_mul(inv, fq_from(r3));
 }
 
+// The same inverse computed by the four lanes of a quad together (all four hold `a`; `mask`
+// covers them).  Every batch's four combinations (f, g, d, e) run one per lane through one code
+// path and are exchanged by shuffles, so a batch costs one combination instead of four on one
+// thread.  All four lanes return the inverse.
+static __device__ __noinline__ fq_t fq_inv_quad(const fq_t &a, uint32_t mask) {
+  const int l = (int)(threadIdx.x & 3);
+  const fq_t c = fq_canon(a);
+  const uint32_t q12[FQ_LIMBS] = BLS_Q;
+  uint32_t f[DS_LIMBS], g[DS_LIMBS], d[DS_LIMBS], e[DS_LIMBS], q[DS_LIMBS];
+  uint32_t nz = 0;
+#pragma unroll
+  for (int i = 0; i < FQ_LIMBS; i++) {
+    f[i] = q[i] = q12[i];
+    g[i] = c.v[i];
+    d[i] = e[i] = 0;
+    nz |= c.v[i];
+  }
+  f[12] = g[12] = d[12] = e[12] = q[12] = 0;
+  e[0] = 1;
+  if (!nz) return fq_zero();
+  int delta = 1;
+#pragma unroll 1
+  for (int batch = 0; batch < 64; batch++) {
+    int32_t u, v, qq, r;
+    delta = ds_batch30(delta, f[0], g[0], u, v, qq, r);
+    // lane 0: f' = (u f + v g) / 2^30, lane 1: g' = (qq f + r g) / 2^30, lanes 2, 3: d', e' mod q
+    uint32_t x[DS_LIMBS], y[DS_LIMBS], res[DS_LIMBS];
+#pragma unroll
+    for (int i = 0; i < DS_LIMBS; i++) {
+      x[i] = l < 2 ? f[i] : d[i];
+      y[i] = l < 2 ? g[i] : e[i];
+    }
+    ds_combine_any(res, (l & 1) ? qq : u, x, (l & 1) ? r : v, y, q, l >= 2);
+    uint32_t gz = 0;
+#pragma unroll
+    for (int i = 0; i < DS_LIMBS; i++) {
+      f[i] = __shfl_sync(mask, res[i], 0, 4);
+      g[i] = __shfl_sync(mask, res[i], 1, 4);
+      d[i] = __shfl_sync(mask, res[i], 2, 4);
+      e[i] = __shfl_sync(mask, res[i], 3, 4);
+      gz |= g[i];
+    }
+    if (gz == 0) break;  // the same on all four lanes
+  }
+  if (ds_is_neg(f)) {  // f = -1: the inverse is q - d
+    int64_t acc = 0;
+#pragma unroll
+    for (int i = 0; i < DS_LIMBS; i++) {
+      acc += (int64_t)q[i] - (int64_t)d[i];
+      d[i] = (uint32_t)acc;
+      acc >>= 32;
+    }
+  }
+  fq_t inv;
+#pragma unroll
+  for (int i = 0; i < FQ_LIMBS; i++) inv.v[i] = d[i];
+  const uint32_t r3[FQ_LIMBS] = BLS_R3;
+  return fq_mul(inv, fq_from(r3));
+}
+
 // ---- 16-byte vector loads/stores of field elements ----
 __device__ __forceinline__ void fq_load(fq_t &r, const uint4 *p) {
 #pragma unroll

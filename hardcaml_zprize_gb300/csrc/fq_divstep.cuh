@@ -151,6 +151,33 @@ FQ_HD void ds_combine_mod(uint32_t (&out)[DS_LIMBS], int32_t a, const uint32_t (
   if (ds_geq(out, q)) ds_add_q(out, q, -1);
 }
 
+// One code path for all four combinations of a batch, so that four lanes of a warp can each take
+// one without diverging: out = (a x + b y) / 2^30, and modulo q when `mod` (x, y in [0, q), result
+// in [0, q)); without `mod`, x and y are signed and the division is exact.
+FQ_HD void ds_combine_any(uint32_t (&out)[DS_LIMBS], int32_t a, const uint32_t (&x)[DS_LIMBS], int32_t b,
+                          const uint32_t (&y)[DS_LIMBS], const uint32_t (&q)[DS_LIMBS], bool mod) {
+  uint32_t w[DS_LIMBS + 1];
+  int64_t acc = 0;
+  for (int i = 0; i < DS_LIMBS; i++) {
+    acc += (int64_t)a * ds_limb(x, i) + (int64_t)b * ds_limb(y, i);
+    w[i] = (uint32_t)acc;
+    acc >>= 32;
+  }
+  w[DS_LIMBS] = (uint32_t)acc;
+  const uint32_t m = mod ? (0u - w[0]) & 0x3fffffffu : 0u;  // a zero multiple of q otherwise
+  int64_t acc2 = 0;
+  for (int i = 0; i < DS_LIMBS; i++) {
+    acc2 += (int64_t)w[i] + (int64_t)m * (int64_t)q[i];
+    w[i] = (uint32_t)acc2;
+    acc2 >>= 32;
+  }
+  w[DS_LIMBS] = (uint32_t)((int64_t)(int32_t)w[DS_LIMBS] + acc2);
+  for (int i = 0; i < DS_LIMBS - 1; i++) out[i] = (w[i] >> 30) | (w[i + 1] << 2);
+  out[DS_LIMBS - 1] = (w[DS_LIMBS - 1] >> 30) | (w[DS_LIMBS] << 2);
+  if (mod && ds_is_neg(out)) ds_add_q(out, q, 1);
+  if (mod && ds_geq(out, q)) ds_add_q(out, q, -1);
+}
+
 // a^-1 mod q as plain integers (12 limbs of 32 bits; a < q; 0 -> 0).  Returns false only if
 // the batch guard ran out, which the divstep bound (at most about 1100 steps for 377 bits,
 // Bernstein-Yang theorem 11.2) rules out.

@@ -1089,12 +1089,17 @@ __global__ void __launch_bounds__(128) k_final(PassBuffers pb) {
   }
   // gather the point on lane 0 (lane 1 holds T, lane 2 Y, lane 3 Z)
   xyzt_t acc;
-  acc.x = dacc;
-  acc.t = dq_xchg(dacc, 1, 0xfu);
-  acc.y = dq_xchg(dacc, 2, 0xfu);
-  acc.z = dq_xchg(dacc, 3, 0xfu);
+  // every lane of the quad takes the whole point (lane 0 holds X, 1 T, 2 Y, 3 Z), and the four
+  // share the inversion of the map to Weierstrass
+#pragma unroll
+  for (int k = 0; k < FQ_LIMBS; k++) {
+    acc.x.v[k] = __shfl_sync(0xfu, dacc.v[k], 0, 4);
+    acc.t.v[k] = __shfl_sync(0xfu, dacc.v[k], 1, 4);
+    acc.y.v[k] = __shfl_sync(0xfu, dacc.v[k], 2, 4);
+    acc.z.v[k] = __shfl_sync(0xfu, dacc.v[k], 3, 4);
+  }
+  wpt_t res = te_to_weierstrass_quad(acc, 0xfu);  // z is 1, or 0 for infinity
   if (threadIdx.x != 0) return;
-  wpt_t res = te_to_weierstrass(acc);  // z is 1, or 0 for infinity
   bool added = false;
   for (uint32_t c = 0; c < pb.n_classes && c < 8; c++) {
     const uint32_t m = cls_sum[c] & 3u;

@@ -1,6 +1,7 @@
 """The divstep inversion (csrc/fq_divstep.cuh) is plain integer C++ shared by host and device;
 this compiles it for the host with g++ and checks it against Python's modular inverse on edge
-values and random values below q.  The device build of the same code is checked through
+values and random values below q, both the one-thread form and the four-lane schedule of
+fq_inv_quad run lane after lane (every value must give the same inverse both ways).  The device build of the same code is checked through
 msm_field_selftest in the GPU suite."""
 import os
 import random
@@ -17,12 +18,43 @@ DRIVER = r"""
 #include <cstdio>
 #include <cstdint>
 #include "%s"
+// the four-lane schedule of fq_inv_quad, one lane after another: each batch's four
+// combinations through ds_combine_any with the lanes' operands
+static bool by_lanes(const uint32_t (&a)[12], const uint32_t (&q12)[12], uint32_t (&out)[12]) {
+  uint32_t f[DS_LIMBS] = {}, g[DS_LIMBS] = {}, d[DS_LIMBS] = {}, e[DS_LIMBS] = {}, q[DS_LIMBS] = {};
+  uint32_t nz = 0;
+  for (int i = 0; i < 12; i++) { f[i] = q[i] = q12[i]; g[i] = a[i]; nz |= a[i]; out[i] = 0; }
+  e[0] = 1;
+  if (!nz) return true;
+  int delta = 1;
+  for (int batch = 0; batch < 64; batch++) {
+    int32_t u, v, qq, r;
+    delta = ds_batch30(delta, f[0], g[0], u, v, qq, r);
+    uint32_t res[4][DS_LIMBS];
+    for (int l = 0; l < 4; l++)
+      ds_combine_any(res[l], (l & 1) ? qq : u, l < 2 ? f : d, (l & 1) ? r : v, l < 2 ? g : e, q, l >= 2);
+    uint32_t gz = 0;
+    for (int i = 0; i < DS_LIMBS; i++) { f[i] = res[0][i]; g[i] = res[1][i]; d[i] = res[2][i]; e[i] = res[3][i]; gz |= g[i]; }
+    if (!gz) {
+      if (ds_is_neg(f)) {
+        int64_t acc = 0;
+        for (int i = 0; i < DS_LIMBS; i++) { acc += (int64_t)q[i] - (int64_t)d[i]; d[i] = (uint32_t)acc; acc >>= 32; }
+      }
+      for (int i = 0; i < 12; i++) out[i] = d[i];
+      return true;
+    }
+  }
+  return false;
+}
 int main() {
   const uint32_t q[12] = {%s};
-  uint32_t a[12], out[12];
+  uint32_t a[12], out[12], out2[12];
   while (fread(a, 4, 12, stdin) == 12) {
-    const bool ok = ds_inverse(a, q, out);
-    fwrite(&ok, 1, 1, stdout);
+    const bool ok = ds_inverse(a, q, out) && by_lanes(a, q, out2);
+    bool same = true;
+    for (int i = 0; i < 12; i++) same &= out[i] == out2[i];
+    const bool all = ok && same;
+    fwrite(&all, 1, 1, stdout);
     fwrite(out, 4, 12, stdout);
   }
   return 0;
