@@ -20,7 +20,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libdriver.so")
-SOURCES = ["msm_pipeline.cu", "msm_aux.cu", "msm_driver.cu", "msm_formats.cpp"]
+SOURCES = ["msm_pipeline.cu", "msm_aux.cu", "msm_driver.cu", "msm_formats.cpp", "ntt.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -50,7 +50,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
 def _build_locked(verbose: bool, force: bool) -> str:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(PKG, "..", "include", "msm_gb300.h"))
+    headers += [os.path.join(PKG, "..", "include", h) for h in ("msm_gb300.h", "ntt_gb300.h")]
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
 
     def compile_one(src):

@@ -1,0 +1,361 @@
+// NTT over the Goldilocks field (p = 2^64 - 2^32 + 1) on sm_103a: the GPU form of the reference's
+// NTT track (zprize/ntt).  The transform is the reference's (zprize/ntt/host/reference.cpp:94-139):
+// X[k] = sum_j x[j] w^(j k) with w = OMEGA[log2 n] of zprize/ntt/host/gf.h:65-99, natural order in
+// and out.  The reference evaluates 2^24 points on the FPGA with the 4-step decomposition into
+// 2^12-point transforms (zprize/ntt/docs/zprize_ntt_top.mld:6-31); this engine does the same split,
+// n = n1 n2 with n1, n2 <= 2^12:
+//   pass A: for every column j1 of the n2 x n1 row-major input, the n2-point transform over j2,
+//           times w^(j1 k2), written to Z[k2][j1];
+//   pass B: for every row k2 of Z, the n1-point transform over j1, written to X[k2 + n2 k1].
+// One kernel does both passes: a block loads C <= 4 of the short transforms into shared memory
+// (bit-reversed positions), runs the log2(m) radix-2 decimation-in-time stages there, and stores
+// them, optionally twisted.  With C = 4 every row of a column load and every output group of a
+// store is 32 contiguous bytes, one DRAM sector.  HBM traffic: n x 8 B read and written per pass.
+// Transforms of at most 2^12 points are one pass.
+//
+// Field arithmetic: elements in [0, p).  The 128-bit product hi 2^64 + lo reduces with
+// 2^64 = 2^32 - 1 and 2^96 = -1 (mod p): hi = hh 2^32 + hl gives lo - hh + hl (2^32 - 1).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/ntt_gb300.h"
+
+namespace {
+
+constexpr uint64_t GL_P = 0xffffffff00000001ull;
+constexpr uint64_t GL_EPS = 0xffffffffull;  // 2^64 mod p
+constexpr uint32_t NTT_MAX_LOG_M = 12;      // longest transform of one block
+constexpr uint32_t NTT_THREADS = 1024;
+
+// 2^i-th roots of unity of the reference's table (gf.h:65-99); OMEGA[i+1]^2 = OMEGA[i]
+const uint64_t GL_OMEGA[33] = {
+    0x0000000000000001ull, 0xffffffff00000000ull, 0x0001000000000000ull, 0xfffffffeff000001ull,
+    0xefffffff00000001ull, 0x00003fffffffc000ull, 0x0000008000000000ull, 0xf80007ff08000001ull,
+    0xbf79143ce60ca966ull, 0x1905d02a5c411f4eull, 0x9d8f2ad78bfed972ull, 0x0653b4801da1c8cfull,
+    0xf2c35199959dfcb6ull, 0x1544ef2335d17997ull, 0xe0ee099310bba1e2ull, 0xf6b2cffe2306baacull,
+    0x54df9630bf79450eull, 0xabd0a6e8aa3d8a0eull, 0x81281a7b05f9beacull, 0xfbd41c6b8caa3302ull,
+    0x30ba2ecd5e93e76dull, 0xf502aef532322654ull, 0x4b2a18ade67246b5ull, 0xea9d5a1336fbc98bull,
+    0x86cdcc31c307e171ull, 0x4bbaf5976ecfefd8ull, 0xed41d05b78d6e286ull, 0x10d78dd8915a171dull,
+    0x59049500004a4485ull, 0xdfa8c93ba46d2666ull, 0x7e9bd009b86a0845ull, 0x400a7f755588e659ull,
+    0x185629dcda58878cull};
+
+// ---- host-side field arithmetic (table set-up) ----
+uint64_t h_mul(uint64_t a, uint64_t b) { return (uint64_t)(((unsigned __int128)a * b) % GL_P); }
+
+// ---- device field arithmetic ----
+__device__ __forceinline__ uint64_t gl_add(uint64_t a, uint64_t b) {
+  const uint64_t s = a + b;
+  if (s < a) return s + GL_EPS;  // a + b - p = s + 2^64 - p, below p
+  return s >= GL_P ? s - GL_P : s;
+}
+__device__ __forceinline__ uint64_t gl_sub(uint64_t a, uint64_t b) {
+  const uint64_t d = a - b;
+  return a < b ? d - GL_EPS : d;  // a - b + p = d - 2^64 + p
+}
+__device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b) {
+  const uint64_t lo = a * b, hi = __umul64hi(a, b);
+  const uint64_t hh = hi >> 32, hl = hi & GL_EPS;
+  uint64_t t0 = lo - hh;
+  if (lo < hh) t0 -= GL_EPS;  // borrow: add p = subtract 2^32 - 1 modulo 2^64
+  const uint64_t t1 = (hl << 32) - hl;
+  uint64_t r = t0 + t1;
+  if (r < t0) r += GL_EPS;  // carry: 2^64 = 2^32 - 1
+  return r >= GL_P ? r - GL_P : r;
+}
+
+__device__ __forceinline__ uint32_t bit_reverse(uint32_t x, uint32_t bits) {
+  return bits ? __brev(x) >> (32 - bits) : 0u;
+}
+
+struct NttPass {
+  const uint64_t *src;
+  uint64_t *dst;
+  uint32_t log_m;  // transform length of this pass
+  uint32_t cols;   // transforms per block (1..4)
+  uint64_t in_c, in_i;    // element i of transform g: src[g in_c + i in_i]
+  uint64_t out_c, out_k;  // output k of transform g: dst[g out_c + k out_k]
+  const uint64_t *tw_m;   // w_m^j, j < m/2
+  // twist (pass A): output k of transform g times w_n^(g k mod n), from w_n^e = hi[e >> 12] lo[e & 4095]
+  const uint64_t *tw_lo, *tw_hi;
+  uint64_t n_mask;  // n - 1 when twisting, 0 otherwise
+};
+
+__global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
+  extern __shared__ uint64_t sm[];
+  const uint32_t m = 1u << ps.log_m, C = ps.cols, half = m >> 1;
+  uint64_t *tw = sm + (size_t)C * m;
+  const uint64_t g0 = (uint64_t)blockIdx.x * C;
+  for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) tw[j] = ps.tw_m[j];
+  // load C transforms, element i to its bit-reversed slot; the unit-stride index runs fastest
+  const bool c_fast = ps.in_c == 1;
+  for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
+    const uint32_t c = c_fast ? t % C : t / m, i = c_fast ? t / C : t % m;
+    uint64_t v = __ldcs(ps.src + (g0 + c) * ps.in_c + (uint64_t)i * ps.in_i);
+    if (v >= GL_P) v -= GL_P;  // inputs are taken modulo p
+    sm[(size_t)c * m + bit_reverse(i, ps.log_m)] = v;
+  }
+  __syncthreads();
+  for (uint32_t s = 1; s <= ps.log_m; s++) {
+    const uint32_t h = 1u << (s - 1);
+    for (uint32_t t = threadIdx.x; t < C * half; t += blockDim.x) {
+      const uint32_t c = t >> (ps.log_m - 1), r = t & (half - 1);
+      const uint32_t j = r & (h - 1), k0 = ((r >> (s - 1)) << s) + j;
+      uint64_t *a = sm + (size_t)c * m;
+      const uint64_t w = tw[j << (ps.log_m - s)];  // w_m^(j m / 2h), a primitive 2h-th root
+      const uint64_t u = a[k0], v = gl_mul(a[k0 + h], w);
+      a[k0] = gl_add(u, v);
+      a[k0 + h] = gl_sub(u, v);
+    }
+    __syncthreads();
+  }
+  // store, output groups of C consecutive transforms together
+  for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
+    const uint32_t c = t % C, k = t / C;
+    uint64_t v = sm[(size_t)c * m + k];
+    if (ps.n_mask) {
+      const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
+      v = gl_mul(v, gl_mul(ps.tw_hi[e >> 12], ps.tw_lo[e & 4095]));
+    }
+    __stcs(ps.dst + (g0 + c) * ps.out_c + (uint64_t)k * ps.out_k, v);
+  }
+}
+
+// Linear copy of n values in 16-byte vectors; the source may be host memory that the device
+// reads through the host's page tables (Grace over NVLink-C2C).
+__global__ void __launch_bounds__(256) k_ntt_copy(const uint4 *src, uint4 *dst, uint64_t nvec) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvec;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// ---- host context ----
+thread_local int g_err = 0;
+thread_local char g_msg[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof(g_msg), fmt, ap);
+  va_end(ap);
+  g_err = code;
+  return code;
+}
+
+#define NCK(x)                                                                            \
+  do {                                                                                    \
+    cudaError_t e_ = (x);                                                                 \
+    if (e_ != cudaSuccess) return fail(NTT_ERR_CUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+  } while (0)
+
+struct NttCtx {
+  int device = 0;
+  uint32_t log_n = 0, log_n1 = 0, log_n2 = 0, cols = 4;
+  uint64_t n = 0;
+  uint64_t *d_in = nullptr, *d_out = nullptr, *d_tmp = nullptr;
+  uint64_t *d_tw1 = nullptr, *d_tw2 = nullptr, *d_twlo = nullptr, *d_twhi = nullptr;
+  // the device reads pageable host memory through the host's page tables: the input vector
+  // moves by a copy kernel instead of a driver copy
+  bool host_direct = false;
+  int num_sms = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[5] = {};
+  bool timing = false;
+  double last_ms[4] = {0, 0, 0, 0};
+  ~NttCtx() {
+    for (uint64_t *p : {d_in, d_out, d_tmp, d_tw1, d_tw2, d_twlo, d_twhi})
+      if (p) cudaFree(p);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+// w^0 .. w^(count - 1)
+std::vector<uint64_t> powers(uint64_t w, uint64_t count) {
+  std::vector<uint64_t> v(std::max<uint64_t>(count, 1));
+  v[0] = 1;
+  for (uint64_t i = 1; i < count; i++) v[i] = h_mul(v[i - 1], w);
+  return v;
+}
+
+int upload(uint64_t **dst, const std::vector<uint64_t> &v) {
+  NCK(cudaMalloc(dst, v.size() * 8));
+  NCK(cudaMemcpy(*dst, v.data(), v.size() * 8, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+size_t pass_smem(uint32_t log_m, uint32_t cols) {
+  return ((size_t)cols * (1u << log_m) + (1u << log_m) / 2 + 1) * 8;
+}
+
+// one pass: `count` transforms of 2^log_m points, `cols` per block
+cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, uint32_t log_m,
+                        uint64_t count, uint64_t in_c, uint64_t in_i, uint64_t out_c, uint64_t out_k,
+                        const uint64_t *tw_m, bool twist, cudaStream_t st) {
+  NttPass ps;
+  ps.src = src;
+  ps.dst = dst;
+  ps.log_m = log_m;
+  ps.cols = (uint32_t)std::min<uint64_t>(cx->cols, count);
+  ps.in_c = in_c;
+  ps.in_i = in_i;
+  ps.out_c = out_c;
+  ps.out_k = out_k;
+  ps.tw_m = tw_m;
+  ps.tw_lo = cx->d_twlo;
+  ps.tw_hi = cx->d_twhi;
+  ps.n_mask = twist ? cx->n - 1 : 0;
+  const uint32_t blocks = (uint32_t)(count / ps.cols);
+  const uint32_t threads = std::min<uint32_t>(NTT_THREADS, std::max<uint32_t>(32, ps.cols << (log_m - (log_m ? 1 : 0))));
+  k_ntt_pass<<<blocks, threads, pass_smem(log_m, ps.cols), st>>>(ps);
+  return cudaGetLastError();
+}
+
+// the transform of cx->n points from d_src to d_dst (device memory), enqueued on st
+int enqueue_ntt(NttCtx *cx, uint64_t *d_dst, const uint64_t *d_src, cudaStream_t st, bool marks) {
+  if (cx->log_n <= NTT_MAX_LOG_M) {
+    NCK(launch_pass(cx, d_src, d_dst, cx->log_n, 1, 0, 1, 0, 1, cx->d_tw1, false, st));
+    if (marks) NCK(cudaEventRecord(cx->ev[2], st));
+    return 0;
+  }
+  const uint64_t n1 = 1ull << cx->log_n1, n2 = 1ull << cx->log_n2;
+  // pass A: n1 columns of n2 points (stride n1), twisted, to Z[k2][j1]
+  NCK(launch_pass(cx, d_src, cx->d_tmp, cx->log_n2, n1, 1, n1, 1, n1, cx->d_tw2, true, st));
+  if (marks) NCK(cudaEventRecord(cx->ev[2], st));
+  // pass B: n2 rows of n1 points, to X[k2 + n2 k1]
+  NCK(launch_pass(cx, cx->d_tmp, d_dst, cx->log_n1, n2, n1, 1, 1, n2, cx->d_tw1, false, st));
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ntt_last_error(char *buf, size_t len) {
+  if (buf && len) {
+    strncpy(buf, g_msg, len - 1);
+    buf[len - 1] = 0;
+  }
+  return g_err;
+}
+
+void *ntt_init(uint32_t log_n) {
+  g_err = 0;
+  if (log_n > 2 * NTT_MAX_LOG_M) {
+    fail(NTT_ERR_ARG, "ntt_init: 2^%u points is over the maximum of 2^%u", log_n, 2 * NTT_MAX_LOG_M);
+    return nullptr;
+  }
+  auto *cx = new NttCtx();
+  const char *dev = getenv("MSM_DEVICE");
+  cx->device = dev ? atoi(dev) : 0;
+  if (const char *c = getenv("NTT_COLS")) {  // transforms per block: 1, 2 or 4
+    const int v = atoi(c);
+    cx->cols = v >= 4 ? 4 : v >= 2 ? 2 : 1;
+  }
+  cx->log_n = log_n;
+  cx->n = 1ull << log_n;
+  cx->log_n2 = log_n / 2;
+  cx->log_n1 = log_n - cx->log_n2;
+  int rc = 0;
+  auto step = [&](cudaError_t e, const char *what) {
+    if (!rc && e != cudaSuccess) rc = fail(NTT_ERR_CUDA, "ntt_init: %s: %s", what, cudaGetErrorString(e));
+  };
+  step(cudaSetDevice(cx->device), "cudaSetDevice");
+  int pageable = 0, host_tables = 0;
+  step(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, cx->device), "attribute");
+  step(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                              cx->device), "attribute");
+  step(cudaDeviceGetAttribute(&cx->num_sms, cudaDevAttrMultiProcessorCount, cx->device), "attribute");
+  const char *hd = getenv("NTT_HOST_DIRECT");
+  cx->host_direct = pageable && host_tables && !(hd && strcmp(hd, "0") == 0);
+  step(cudaStreamCreateWithFlags(&cx->st, cudaStreamNonBlocking), "stream");
+  for (auto &e : cx->ev) step(cudaEventCreate(&e), "event");
+  step(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)pass_smem(NTT_MAX_LOG_M, 4)),
+       "shared memory size");
+  step(cudaMalloc(&cx->d_in, cx->n * 8), "input buffer");
+  step(cudaMalloc(&cx->d_out, cx->n * 8), "output buffer");
+  if (log_n > NTT_MAX_LOG_M) step(cudaMalloc(&cx->d_tmp, cx->n * 8), "intermediate buffer");
+  if (!rc) {
+    // short-transform roots: w_m = w_n^(n/m), from the reference's table
+    const uint32_t l1 = log_n > NTT_MAX_LOG_M ? cx->log_n1 : log_n;
+    rc = upload(&cx->d_tw1, powers(GL_OMEGA[l1], (1ull << l1) / 2));
+    if (!rc && log_n > NTT_MAX_LOG_M) {
+      rc = upload(&cx->d_tw2, powers(GL_OMEGA[cx->log_n2], (1ull << cx->log_n2) / 2));
+      const uint64_t w = GL_OMEGA[log_n];
+      if (!rc) rc = upload(&cx->d_twlo, powers(w, std::min<uint64_t>(cx->n, 4096)));
+      uint64_t w4096 = w;
+      for (int i = 0; i < 12; i++) w4096 = h_mul(w4096, w4096);
+      if (!rc) rc = upload(&cx->d_twhi, powers(w4096, std::max<uint64_t>(cx->n >> 12, 1)));
+    }
+  }
+  if (rc) {
+    delete cx;
+    return nullptr;
+  }
+  return cx;
+}
+
+void ntt_free(void *context) { delete (NttCtx *)context; }
+
+uint64_t ntt_input_vector_size(void *context) {
+  return context ? ((NttCtx *)context)->n : 0;
+}
+
+int ntt_evaluate_device(void *context, uint64_t *d_out, const uint64_t *d_in, void *stream) {
+  g_err = 0;
+  auto *cx = (NttCtx *)context;
+  if (!cx || !d_out || !d_in) return fail(NTT_ERR_ARG, "ntt_evaluate_device: null argument");
+  if (d_out == d_in && cx->log_n <= NTT_MAX_LOG_M)
+    return fail(NTT_ERR_ARG, "ntt_evaluate_device: the transform is out of place");
+  NCK(cudaSetDevice(cx->device));
+  return enqueue_ntt(cx, d_out, d_in, stream ? (cudaStream_t)stream : cx->st, false);
+}
+
+int ntt_evaluate(void *context, uint64_t *out, const uint64_t *in, uint64_t len) {
+  g_err = 0;
+  auto *cx = (NttCtx *)context;
+  if (!cx || !out || !in) return fail(NTT_ERR_ARG, "ntt_evaluate: null argument");
+  if (len != cx->n)
+    return fail(NTT_ERR_ARG, "ntt_evaluate: %llu values for a transform of %llu points",
+                (unsigned long long)len, (unsigned long long)cx->n);
+  NCK(cudaSetDevice(cx->device));
+  // A copy kernel reads the input when the device reaches pageable memory and the buffer is
+  // 16-byte aligned (GB300 at 2^24: 0.67 ms against 0.77 ms for the driver's copy); otherwise the
+  // driver copies it.  The output always goes back through the driver: a kernel writing into
+  // pages the host has not touched yet takes a fault per page (29 ms at 2^24 against 4.9 ms).
+  const bool direct = cx->host_direct && cx->n >= 2 && ((uintptr_t)in & 15) == 0;
+  const uint32_t cblocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)cx->num_sms * 8, cx->n / 512));
+  NCK(cudaEventRecord(cx->ev[0], cx->st));
+  if (direct) {
+    k_ntt_copy<<<cblocks, 256, 0, cx->st>>>((const uint4 *)in, (uint4 *)cx->d_in, cx->n / 2);
+    NCK(cudaGetLastError());
+  } else {
+    NCK(cudaMemcpyAsync(cx->d_in, in, cx->n * 8, cudaMemcpyHostToDevice, cx->st));
+  }
+  NCK(cudaEventRecord(cx->ev[1], cx->st));
+  if (int rc = enqueue_ntt(cx, cx->d_out, cx->d_in, cx->st, true)) return rc;
+  NCK(cudaEventRecord(cx->ev[3], cx->st));
+  NCK(cudaMemcpyAsync(out, cx->d_out, cx->n * 8, cudaMemcpyDeviceToHost, cx->st));
+  NCK(cudaEventRecord(cx->ev[4], cx->st));
+  NCK(cudaStreamSynchronize(cx->st));
+  float ms[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 4; k++) cudaEventElapsedTime(&ms[k], cx->ev[k], cx->ev[k + 1]);
+  for (int k = 0; k < 4; k++) cx->last_ms[k] = ms[k];
+  return 0;
+}
+
+int ntt_last_timings(void *context, double *ms, int32_t max_stages) {
+  auto *cx = (NttCtx *)context;
+  if (!cx || !ms) return fail(NTT_ERR_ARG, "ntt_last_timings: null argument");
+  const int k = std::min<int32_t>(max_stages, 4);
+  for (int i = 0; i < k; i++) ms[i] = cx->last_ms[i];
+  return k;
+}
+
+}  // extern "C"

@@ -36,6 +36,16 @@ def lib():
         L.oracle_rand_u64.restype = U64
         L.oracle_gen_scalars.argtypes = [U64, U64, I, U64, P, I]
         L.oracle_gen_scalars.restype = I
+        L.oracle_ntt.argtypes = [P, P, I, I]
+        L.oracle_ntt.restype = I
+        L.oracle_intt.argtypes = [P, P, I, I]
+        L.oracle_intt.restype = I
+        L.oracle_gl_mul.argtypes = [U64, U64]
+        L.oracle_gl_mul.restype = U64
+        L.oracle_gl_omega.argtypes = [I]
+        L.oracle_gl_omega.restype = U64
+        L.oracle_mt19937_64.argtypes = [U64, P, U64, I]
+        L.oracle_mt19937_64.restype = I
         _lib = L
     return _lib
 
@@ -75,3 +85,38 @@ def mul(point: np.ndarray, k: int) -> np.ndarray:
 
 def default_window(n: int) -> int:
     return lib().oracle_default_window(n)
+
+
+# ---- NTT track (Goldilocks field) ----
+GL_P = 0xFFFFFFFF00000001
+
+
+def ntt(values: np.ndarray, threads: int = 0, inverse: bool = False) -> np.ndarray:
+    """Forward (or inverse) NTT of 2^k Goldilocks elements, natural order in and out
+    (oracle/cpu_ntt.c; the reference's host model zprize/ntt/host/reference.cpp:94-139)."""
+    x = np.ascontiguousarray(values, dtype=np.uint64).reshape(-1)
+    n = x.shape[0]
+    logn = n.bit_length() - 1
+    if n == 0 or (1 << logn) != n:
+        raise ValueError("the NTT length must be a power of two")
+    out = np.empty_like(x)
+    fn = lib().oracle_intt if inverse else lib().oracle_ntt
+    if fn(out.ctypes.data, x.ctypes.data, logn, threads) != 0:
+        raise ValueError("unsupported NTT length")
+    return out
+
+
+def gl_mul(a: int, b: int) -> int:
+    return int(lib().oracle_gl_mul(a, b))
+
+
+def gl_omega(i: int) -> int:
+    return int(lib().oracle_gl_omega(i))
+
+
+def mt19937_64(n: int, seed: int = 5489, mod_p: bool = True) -> np.ndarray:
+    """n draws of MT19937-64 (std::mt19937_64; 5489 is its default seed), taken modulo p as the
+    reference host's NTT test does (zprize/ntt/host/test_random.cpp)."""
+    out = np.empty(n, dtype=np.uint64)
+    lib().oracle_mt19937_64(seed, out.ctypes.data, n, 1 if mod_p else 0)
+    return out

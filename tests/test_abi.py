@@ -25,6 +25,24 @@ def test_exports_every_declared_symbol(engine):
     assert sorted(engine.EXPORTED) == names
 
 
+def test_ntt_exports_every_declared_symbol(engine):
+    from hardcaml_zprize_gb300 import ntt
+    text = open(os.path.join(ROOT, "include", "ntt_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(ntt_[a-z_0-9]+)\s*\(", text)))
+    assert "ntt_init" in names and "ntt_evaluate" in names
+    lib = engine.load_library()
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(ntt.EXPORTED) == names
+
+
+def test_ntt_argument_errors(engine):
+    from hardcaml_zprize_gb300 import ntt
+    with pytest.raises(engine.MsmError, match="maximum"):
+        ntt.NttContext(25)
+
+
 def test_struct_layout_matches_harness(engine):
     # rust_types.h:8-83; the library static_asserts the same sizes
     assert engine.AFFINE_BYTES == 104 and engine.PROJ_BYTES == 144 and engine.SCALAR_BYTES == 32

@@ -1,0 +1,113 @@
+"""The GPU NTT (ntt_* entry points) against the oracle, bit-exact, at every size up to 2^24.
+
+Expected values come from oracle/cpu_ntt.c, itself pinned to the reference's root table and
+committed transform vectors (tests/test_ntt_oracle.py).  The inputs include the two cases the
+reference host's test draws (zprize/ntt/host/test_random.cpp: a vector of ones, and
+std::mt19937_64 draws taken modulo p), the reference model's committed vectors, edge values
+(0, 1, p - 1) and inputs at or above p, which the engine takes modulo p.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+P = 0xFFFFFFFF00000001
+
+
+@pytest.fixture(scope="module")
+def ntt_mod(engine):
+    from hardcaml_zprize_gb300 import ntt
+    return ntt
+
+
+def random_below_p(rng, n):
+    hi = rng.integers(0, 2**32, n, dtype=np.uint64)
+    lo = rng.integers(0, 2**32, n, dtype=np.uint64)
+    return ((hi << np.uint64(32)) | lo) % np.uint64(P)
+
+
+@pytest.mark.parametrize("log_n", [0, 1, 2, 3, 4, 7, 10, 12, 13, 15, 16, 18, 20, 21])
+def test_ntt_matches_oracle(ntt_mod, ocpu, log_n):
+    rng = np.random.default_rng(100 + log_n)
+    x = random_below_p(rng, 1 << log_n)
+    x[0] = P - 1
+    if x.size > 2:
+        x[1], x[2] = 0, 1
+    ctx = ntt_mod.NttContext(log_n)
+    try:
+        assert ctx.input_vector_size() == 1 << log_n
+        want = ocpu.ntt(x)
+        assert np.array_equal(ctx.evaluate(x), want)
+        assert np.array_equal(ctx.evaluate(x), want)  # a second call on the same context
+    finally:
+        ctx.close()
+
+
+def test_reference_model_vectors(ntt_mod):
+    with open(os.path.join(ROOT, "tests", "golden", "ntt_kats.json")) as f:
+        v = json.load(f)["vectors"]
+    ctx = ntt_mod.NttContext(3)
+    try:
+        for key in ("ntt8_of_1_2", "ntt8_random"):
+            x = np.array([int(t, 16) for t in v[key]["input"]], dtype=np.uint64)
+            assert [int(t) for t in ctx.evaluate(x)] == [int(t, 16) for t in v[key]["output"]], key
+    finally:
+        ctx.close()
+    ctx = ntt_mod.NttContext(12)
+    try:
+        x = np.zeros(4096, dtype=np.uint64)
+        x[0], x[1] = 1, 2
+        got = ctx.evaluate(x)
+        assert [int(t) for t in got[:8]] == [int(t, 16) for t in v["ntt4096_of_1_2_first8"]["output_first"]]
+    finally:
+        ctx.close()
+
+
+def test_reference_test_inputs_at_2_24(ntt_mod, ocpu):
+    """The reference host test's two cases at the contest size: ones, and mt19937_64 % p."""
+    n = 1 << 24
+    ctx = ntt_mod.NttContext(24)
+    try:
+        out = ctx.evaluate(np.ones(n, dtype=np.uint64))
+        assert int(out[0]) == n and not out[1:].any()
+        x = ocpu.mt19937_64(n)
+        assert np.array_equal(ctx.evaluate(x), ocpu.ntt(x, threads=os.cpu_count() or 1))
+    finally:
+        ctx.close()
+
+
+def test_inputs_at_or_above_p_are_reduced(ntt_mod, ocpu):
+    rng = np.random.default_rng(7)
+    x = random_below_p(rng, 1 << 14)
+    y = x.copy()
+    y[::3] += np.uint64(P) * (y[::3] < np.uint64(2**64 - P))  # x + p where it fits in 64 bits
+    y[5] = np.uint64(2**64 - 1)
+    x[5] = np.uint64((2**64 - 1) % P)
+    ctx = ntt_mod.NttContext(14)
+    try:
+        assert np.array_equal(ctx.evaluate(y), ocpu.ntt(x))
+    finally:
+        ctx.close()
+
+
+def test_device_entry_point_and_roundtrip(ntt_mod, ocpu):
+    import torch
+    log_n = 20
+    rng = np.random.default_rng(11)
+    x = random_below_p(rng, 1 << log_n)
+    ctx = ntt_mod.NttContext(log_n)
+    try:
+        d_in = torch.from_numpy(x.view(np.int64)).cuda()
+        d_out = torch.empty_like(d_in)
+        torch.cuda.synchronize()
+        ctx.evaluate_device(d_out.data_ptr(), d_in.data_ptr())
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, ctx.evaluate(x))
+        assert np.array_equal(ocpu.ntt(got, inverse=True), x)  # the oracle's inverse undoes it
+    finally:
+        ctx.close()
