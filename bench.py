@@ -13,7 +13,9 @@ step.  Inputs are synthetic and seeded; scalar and base buffers (512 MB + 2.4 GB
          the served mix (Poisson arrivals, sizes 2^12..2^22 over a 2^22 base set), the oracle
          port timed on the host cores, the same 2^24 MSM over the plain resident form (144 B
          per base, no tables: `plain_144B_per_base`) and the fixed-base large MSM (4 x 2^26
-         over one resident base set, batch 0 checked against the oracle: `fixed_base_4x`).
+         over one resident base set, batch 0 checked against the oracle: `fixed_base_4x`), and the
+         NTT track (one 2^24-point Goldilocks NTT, device and host to host, checked against the
+         oracle: `ntt`).
 
 `--impl reference` times the CPU port of the reference's oracle algorithm (arkworks-style
 Pippenger, oracle/cpu_msm.c) on all host cores on the same workload; the reference itself
@@ -366,6 +368,9 @@ def run_ours(args, rank, world, local):
         line["plain_144B_per_base"] = bench_plain_form(args, eng, torch, dev, pts, dev_sc, last_sc,
                                                        out_cpu, peak_imad, local)
     del pts
+    # ---- the NTT track: one 2^24-point Goldilocks NTT per step ----
+    if not args.skip_ntt and rank == 0:
+        line["ntt"] = bench_ntt(args, args.ntt_log2n, local, check=not args.skip_cpu)
     # ---- fixed-base large MSM: 4 x 2^26 over one resident base set ----
     if not args.skip_large and rank == 0:
         line["fixed_base_4x"] = fixed_base_large(args, eng, peaks, local, 26, check=not args.skip_cpu)
@@ -522,6 +527,105 @@ def fixed_base_large(args, eng, peaks, local, log2n, check=True):
         "reference_fpga": {"total_s": 20.336, "msm_per_s": 4 / 20.336,
                            "source": "reference README: 4 x 2^26 in 20.336 s on AWS F1 (not run here)"},
     }
+
+
+def bench_ntt(args, log_n, local, check=True):
+    """The NTT track at the reference's contest size: one Goldilocks NTT of 2^log_n points per
+    step (4-step, two shared-memory passes), on device buffers (`device`) and host to host through
+    ntt_evaluate (`e2e`, input read over NVLink-C2C by a copy kernel, output copied back into a
+    populated buffer).  The roofline is HBM: each pass reads and writes the vector once
+    (2 x 8 B per point).  Inputs are the reference host test's kind (zprize/ntt/host/
+    test_random.cpp): uniform values below p, seeded."""
+    import torch
+    from hardcaml_zprize_gb300 import ntt
+    n = 1 << log_n
+    rng = np.random.default_rng(args.seed + 13)
+    hi = rng.integers(0, 2**32, n, dtype=np.uint64)
+    x = ((hi << np.uint64(32)) | rng.integers(0, 2**32, n, dtype=np.uint64)) % np.uint64(ntt.GL_P)
+    ctx = ntt.NttContext(log_n)
+    try:
+        d_in = torch.from_numpy(x.view(np.int64)).cuda()
+        d_out = torch.empty_like(d_in)
+        for _ in range(args.warmup):
+            ctx.evaluate_device(d_out.data_ptr(), d_in.data_ptr())
+        torch.cuda.synchronize()
+        steps = max(args.steps, 10)
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                ctx.evaluate_device(d_out.data_ptr(), d_in.data_ptr())
+            torch.cuda.synchronize()
+            t_dev = (time.perf_counter() - t0) / steps
+        out = np.zeros(n, dtype=np.uint64)
+        for _ in range(args.warmup):
+            ctx.evaluate(x, out=out)
+        stages = {}
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.evaluate(x, out=out)
+            for k, v in ctx.last_timings().items():
+                stages[k] = stages.get(k, 0.0) + v / steps
+        t_e2e = (time.perf_counter() - t0) / steps
+        same = bool(np.array_equal(out, d_out.cpu().numpy().view(np.uint64)))
+    finally:
+        ctx.close()
+    peak, src = 6800.0, "fallback 6.8 TB/s"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        pass
+    pass_ms = [stages.get("pass_a", 0), stages.get("pass_b", 0)]
+    alg = 2 * n * 8  # one read and one write of the vector per pass
+    res = {
+        "workload": f"Goldilocks NTT, 2^{log_n} points, natural order in and out",
+        "n": n, "device": {"value": 1.0 / t_dev, "unit": "NTT/s", "ms_per_ntt": 1e3 * t_dev},
+        "e2e": {"value": 1.0 / t_e2e, "unit": "NTT/s", "ms_per_ntt": 1e3 * t_e2e,
+                "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
+        "stages_ms": stages,
+        "roofline": {"bound": "hbm", "kernel": "k_ntt_pass", "unit": "GB/s", "peak": peak,
+                     "peak_source": src, "algorithmic_bytes_per_launch": alg,
+                     "achieved": [alg / (t * 1e-3) / 1e9 if t else None for t in pass_ms],
+                     "frac": [alg / (t * 1e-3) / 1e9 / peak if t else None for t in pass_ms]},
+        "device_equals_host_path": same,
+        "clocks": clk.summary(),
+        "reference_fpga": {"ntt_s": [0.0267, 0.0450], "e2e_s": [0.168, 0.177],
+                           "source": "reference docs/zprize_ntt_top.mld: 64-core builds, optimized and "
+                                     "normal layout; evaluate with host pre/post-processing (not run here)"},
+    }
+    if check:
+        from oracle import cpu as ocpu
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        want = ocpu.ntt(x, threads=cores)
+        t_cpu = time.perf_counter() - t0
+        res["parity_vs_cpu"] = bool(np.array_equal(out, want))
+        res["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "NTT/s", "cores": cores, "kind": "port",
+                               "sample": f"one NTT of 2^{log_n} points (oracle/cpu_ntt.c: the reference's "
+                                         f"radix-2 host model, stages parallel over OpenMP)"}
+    return res
+
+
+def run_ntt(args, rank, world, local):
+    """`--workload ntt`: the NTT block alone, as its own line."""
+    from hardcaml_zprize_gb300 import build
+    build.build()
+    os.environ["MSM_DEVICE"] = str(local)
+    if rank != 0:
+        return
+    res = bench_ntt(args, args.ntt_log2n, local, check=not args.skip_cpu)
+    line = {
+        "metric": "ntt_per_s", "value": res["device"]["value"], "unit": "NTT/s", "n_gpus": world,
+        "steps": max(args.steps, 10), "warmup": args.warmup, "ms_per_step": res["device"]["ms_per_ntt"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded uniform values below p)",
+        "config": {"workload": res["workload"], "n": res["n"]},
+        "e2e": {k: res["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
+        "roofline": res["roofline"], "clocks": res["clocks"], "ntt": res,
+    }
+    if "cpu_baseline" in res:
+        line["cpu_baseline"] = res["cpu_baseline"]
+    print(json.dumps(line), flush=True)
 
 
 def run_fixed_base_large(args, rank, world, local):
@@ -754,6 +858,8 @@ def main():
     ap.add_argument("--skip-plain-form", action="store_true",
                     help="skip the 144 B-per-base (no tables) form of the headline MSM")
     ap.add_argument("--skip-large", action="store_true", help="skip the 4 x 2^26 fixed-base block")
+    ap.add_argument("--skip-ntt", action="store_true", help="skip the NTT block")
+    ap.add_argument("--ntt-log2n", type=int, default=24)
     ap.add_argument("--tune-budget-ms", type=int, default=15000,
                     help="time the batch autotuner may spend on the uneven mix (0: skip it)")
     ap.add_argument("--served-requests", type=int, default=48)
@@ -761,7 +867,7 @@ def main():
     ap.add_argument("--served-budget-gb", type=int, default=16)
     ap.add_argument("--served-inflight", type=int, nargs="*", default=[2, 4],
                     help="server slots (passes in flight) to sweep at each offered load")
-    ap.add_argument("--workload", default="plain", choices=["plain", "fixed_base_4x", "sharded"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "fixed_base_4x", "sharded", "ntt"],
                     help="plain: the default single-MSM line; fixed_base_4x: 4 MSMs over one "
                          "resident base set (use with --log2n 26); sharded: one MSM split over "
                          "the ranks by base slices")
@@ -774,6 +880,8 @@ def main():
         run_fixed_base_large(args, rank, world, local)
     elif args.workload == "sharded":
         run_sharded(args, rank, world, local)
+    elif args.workload == "ntt":
+        run_ntt(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
     if world > 1:

@@ -125,6 +125,104 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
   }
 }
 
+// ---- radix-8 decimation in frequency (the pass kernel) ----
+// Natural order in, bit-reversed order in shared memory out: stage H (half size) turns the pair
+// (k, k + H) of each block of 2H into (u + v, (u - v) w_2H^(k mod H)).  Three consecutive stages
+// only mix the 8 elements {b 2H0 + j + t h : t < 8} (h = H0 / 4), so each round of three stages
+// runs in registers: one shared-memory load and store per element per round instead of one per
+// stage, and the first round reads global memory directly (natural order: coalesced).  The last
+// step gathers X[k] = a[rev(k)].  Slots are swizzled (low four bits XOR bits 4..7 and 8..11) and
+// transforms sit 8 slots apart, which makes the rounds' and the gather's 64-bit accesses free of
+// bank conflicts for m = 4096.
+__device__ __forceinline__ uint32_t slot(uint32_t q) { return q ^ ((q >> 4) & 15u) ^ ((q >> 8) & 15u); }
+
+template <int R>
+__device__ __forceinline__ void dif_unit(uint64_t (&x)[8], uint32_t j, uint32_t log_hmin,
+                                         uint32_t log_m, const uint64_t *tw) {
+#pragma unroll
+  for (int l = 0; l < R; l++) {
+    const int d = 1 << (R - 1 - l);                    // partner distance within the unit
+    const uint32_t log_h = log_hmin + (R - 1 - l);     // this stage's half size
+#pragma unroll
+    for (int t = 0; t < (1 << R); t++) {
+      if (t & d) continue;
+      const uint32_t jp = j + ((uint32_t)(t & (d - 1)) << log_hmin);  // position within the half
+      const uint64_t w = tw[jp << (log_m - 1 - log_h)];              // w_2H^jp = w_m^(jp m / 2H)
+      const uint64_t u = x[t], v = x[t + d];
+      x[t] = gl_add(u, v);
+      x[t + d] = gl_mul(gl_sub(u, v), w);
+    }
+  }
+}
+
+// One round of R stages over every unit of the block's transforms; the first round reads the
+// transforms from global memory (natural order), the others from shared memory.
+template <int R>
+__device__ __forceinline__ void dif_round(const NttPass &ps, uint64_t *sm, uint32_t pitch,
+                                          const uint64_t *tw, uint32_t log_hmin, bool from_global) {
+  const uint32_t m = 1u << ps.log_m, C = ps.cols, units = m >> R;
+  const uint64_t g0 = (uint64_t)blockIdx.x * C;
+  const bool c_fast = from_global && ps.in_c == 1;  // consecutive lanes on consecutive transforms
+  for (uint32_t w = threadIdx.x; w < C * units; w += blockDim.x) {
+    const uint32_t c = c_fast ? w % C : w / units, u = c_fast ? w / C : w % units;
+    const uint32_t j = u & ((1u << log_hmin) - 1), b = u >> log_hmin;
+    const uint32_t q0 = (b << (log_hmin + R)) + j;
+    uint64_t x[8];
+    uint64_t *a = sm + (size_t)c * pitch;
+#pragma unroll
+    for (int t = 0; t < (1 << R); t++) {
+      const uint32_t q = q0 + ((uint32_t)t << log_hmin);
+      if (from_global) {
+        uint64_t v = __ldcs(ps.src + (g0 + c) * ps.in_c + (uint64_t)q * ps.in_i);
+        x[t] = v >= GL_P ? v - GL_P : v;  // inputs are taken modulo p
+      } else {
+        x[t] = a[slot(q)];
+      }
+    }
+    dif_unit<R>(x, j, log_hmin, ps.log_m, tw);
+#pragma unroll
+    for (int t = 0; t < (1 << R); t++) a[slot(q0 + ((uint32_t)t << log_hmin))] = x[t];
+  }
+}
+
+__global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass8(NttPass ps) {
+  extern __shared__ uint64_t sm[];
+  const uint32_t m = 1u << ps.log_m, C = ps.cols, half = m >> 1, pitch = m + 8;
+  uint64_t *tw = sm + (size_t)C * pitch;
+  const uint64_t g0 = (uint64_t)blockIdx.x * C;
+  for (uint32_t j = threadIdx.x; j < half; j += blockDim.x) tw[j] = ps.tw_m[j];
+  __syncthreads();
+  int log_h0 = (int)ps.log_m - 1;  // half size of the next stage
+  bool first = true;
+  while (log_h0 >= 0) {
+    const int r = log_h0 + 1 >= 3 ? 3 : log_h0 + 1;
+    const uint32_t log_hmin = (uint32_t)(log_h0 - (r - 1));
+    if (r == 3) dif_round<3>(ps, sm, pitch, tw, log_hmin, first);
+    else if (r == 2) dif_round<2>(ps, sm, pitch, tw, log_hmin, first);
+    else dif_round<1>(ps, sm, pitch, tw, log_hmin, first);
+    __syncthreads();
+    first = false;
+    log_h0 -= r;
+  }
+  if (first) {  // m = 1: no stage, the value itself
+    for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+      const uint64_t v = __ldcs(ps.src + (g0 + c) * ps.in_c);
+      sm[(size_t)c * pitch] = v >= GL_P ? v - GL_P : v;
+    }
+    __syncthreads();
+  }
+  // gather in natural order, output groups of C consecutive transforms together
+  for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
+    const uint32_t c = t % C, k = t / C;
+    uint64_t v = sm[(size_t)c * pitch + slot(bit_reverse(k, ps.log_m))];
+    if (ps.n_mask) {
+      const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
+      v = gl_mul(v, gl_mul(ps.tw_hi[e >> 12], ps.tw_lo[e & 4095]));
+    }
+    __stcs(ps.dst + (g0 + c) * ps.out_c + (uint64_t)k * ps.out_k, v);
+  }
+}
+
 // Linear copy of n values in 16-byte vectors; the source may be host memory that the device
 // reads through the host's page tables (Grace over NVLink-C2C).
 __global__ void __launch_bounds__(256) k_ntt_copy(const uint4 *src, uint4 *dst, uint64_t nvec) {
@@ -161,6 +259,7 @@ struct NttCtx {
   // the device reads pageable host memory through the host's page tables: the input vector
   // moves by a copy kernel instead of a driver copy
   bool host_direct = false;
+  bool radix2 = false;  // the radix-2 pass kernel (comparison)
   int num_sms = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev[5] = {};
@@ -190,7 +289,7 @@ int upload(uint64_t **dst, const std::vector<uint64_t> &v) {
 }
 
 size_t pass_smem(uint32_t log_m, uint32_t cols) {
-  return ((size_t)cols * (1u << log_m) + (1u << log_m) / 2 + 1) * 8;
+  return ((size_t)cols * ((1u << log_m) + 8) + (1u << log_m) / 2 + 1) * 8;
 }
 
 // one pass: `count` transforms of 2^log_m points, `cols` per block
@@ -212,7 +311,10 @@ cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, ui
   ps.n_mask = twist ? cx->n - 1 : 0;
   const uint32_t blocks = (uint32_t)(count / ps.cols);
   const uint32_t threads = std::min<uint32_t>(NTT_THREADS, std::max<uint32_t>(32, ps.cols << (log_m - (log_m ? 1 : 0))));
-  k_ntt_pass<<<blocks, threads, pass_smem(log_m, ps.cols), st>>>(ps);
+  if (cx->radix2)
+    k_ntt_pass<<<blocks, threads, pass_smem(log_m, ps.cols), st>>>(ps);
+  else
+    k_ntt_pass8<<<blocks, threads, pass_smem(log_m, ps.cols), st>>>(ps);
   return cudaGetLastError();
 }
 
@@ -278,6 +380,10 @@ void *ntt_init(uint32_t log_n) {
   step(cudaFuncSetAttribute(k_ntt_pass, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             (int)pass_smem(NTT_MAX_LOG_M, 4)),
        "shared memory size");
+  step(cudaFuncSetAttribute(k_ntt_pass8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)pass_smem(NTT_MAX_LOG_M, 4)),
+       "shared memory size");
+  if (const char *r2 = getenv("NTT_RADIX2")) cx->radix2 = strcmp(r2, "1") == 0;
   step(cudaMalloc(&cx->d_in, cx->n * 8), "input buffer");
   step(cudaMalloc(&cx->d_out, cx->n * 8), "output buffer");
   if (log_n > NTT_MAX_LOG_M) step(cudaMalloc(&cx->d_tmp, cx->n * 8), "intermediate buffer");
