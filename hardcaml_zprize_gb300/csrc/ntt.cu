@@ -48,24 +48,83 @@ const uint64_t GL_OMEGA[33] = {
 uint64_t h_mul(uint64_t a, uint64_t b) { return (uint64_t)(((unsigned __int128)a * b) % GL_P); }
 
 // ---- device field arithmetic ----
+// Carry-chain forms on 32-bit halves: every correction is driven by a carry or borrow flag, so no
+// 64-bit comparison or select chain is needed.  Inputs and outputs are canonical (below p).
+__device__ __forceinline__ uint64_t gl_pack(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
+
+// a + b: S = a + b < 2p; S >= p exactly when S + (2^32 - 1) carries out of 64 bits (counting
+// the first carry), and then S - p = (S + 2^32 - 1) mod 2^64
 __device__ __forceinline__ uint64_t gl_add(uint64_t a, uint64_t b) {
-  const uint64_t s = a + b;
-  if (s < a) return s + GL_EPS;  // a + b - p = s + 2^64 - p, below p
-  return s >= GL_P ? s - GL_P : s;
+  uint32_t s0, s1, t0, t1, c;
+  asm("{\n\t.reg .u32 c1;\n\t"
+      "add.cc.u32 %0, %5, %7;\n\t"
+      "addc.cc.u32 %1, %6, %8;\n\t"
+      "addc.u32 c1, 0, 0;\n\t"
+      "add.cc.u32 %2, %0, 0xffffffff;\n\t"
+      "addc.cc.u32 %3, %1, 0;\n\t"
+      "addc.u32 %4, c1, 0;\n\t}"
+      : "=&r"(s0), "=&r"(s1), "=&r"(t0), "=&r"(t1), "=&r"(c)
+      : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+  return c ? gl_pack(t0, t1) : gl_pack(s0, s1);
 }
+
+// a - b: on a borrow the wrapped difference d = a - b + 2^64 >= 2^32, and d - (2^32 - 1) is
+// a - b + p
 __device__ __forceinline__ uint64_t gl_sub(uint64_t a, uint64_t b) {
-  const uint64_t d = a - b;
-  return a < b ? d - GL_EPS : d;  // a - b + p = d - 2^64 + p
+  uint32_t d0, d1;
+  asm("{\n\t.reg .u32 bw;\n\t"
+      "sub.cc.u32 %0, %2, %4;\n\t"
+      "subc.cc.u32 %1, %3, %5;\n\t"
+      "subc.u32 bw, 0, 0;\n\t"
+      "sub.cc.u32 %0, %0, bw;\n\t"
+      "subc.u32 %1, %1, 0;\n\t}"
+      : "=&r"(d0), "=&r"(d1)
+      : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+  return gl_pack(d0, d1);
 }
+
+// a b: the 128-bit product (r3 r2 r1 r0) from four wide multiplies, then
+// lo - hh + hl (2^32 - 1) with lo = r1 r0, hl = r2, hh = r3 (2^64 = 2^32 - 1, 2^96 = -1), each
+// step corrected by its own carry or borrow, and a last conditional subtraction of p
 __device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b) {
-  const uint64_t lo = a * b, hi = __umul64hi(a, b);
-  const uint64_t hh = hi >> 32, hl = hi & GL_EPS;
-  uint64_t t0 = lo - hh;
-  if (lo < hh) t0 -= GL_EPS;  // borrow: add p = subtract 2^32 - 1 modulo 2^64
-  const uint64_t t1 = (hl << 32) - hl;
-  uint64_t r = t0 + t1;
-  if (r < t0) r += GL_EPS;  // carry: 2^64 = 2^32 - 1
-  return r >= GL_P ? r - GL_P : r;
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+  const uint64_t x = (uint64_t)a0 * b0, y = (uint64_t)a0 * b1, z = (uint64_t)a1 * b0,
+                 w = (uint64_t)a1 * b1;
+  uint32_t r0, r1, t0, t1, c;
+  asm("{\n\t.reg .u32 r2, r3, m, u0, u1, q0, q1;\n\t"
+      // r1 r2 r3 = x.hi + y + z 2^0 + w 2^32 aligned: (r3 r2 r1 r0) = x + (y + z) 2^32 + w 2^64
+      "add.cc.u32 %1, %6, %7;\n\t"        // r1 = x.hi + y.lo
+      "addc.cc.u32 r2, %12, %8;\n\t"      // r2 = w.lo + y.hi
+      "addc.u32 r3, %13, 0;\n\t"          // r3 = w.hi
+      "add.cc.u32 %1, %1, %9;\n\t"        // r1 += z.lo
+      "addc.cc.u32 r2, r2, %10;\n\t"      // r2 += z.hi
+      "addc.u32 r3, r3, 0;\n\t"
+      // t = lo - hh, on a borrow subtract 2^32 - 1 more
+      "sub.cc.u32 %2, %5, r3;\n\t"
+      "subc.cc.u32 %3, %1, 0;\n\t"
+      "subc.u32 m, 0, 0;\n\t"
+      "sub.cc.u32 %2, %2, m;\n\t"
+      "subc.u32 %3, %3, 0;\n\t"
+      // u = hl (2^32 - 1) = hl 2^32 - hl
+      "sub.cc.u32 u0, 0, r2;\n\t"
+      "subc.u32 u1, r2, 0;\n\t"
+      // t += u, on a carry add 2^32 - 1
+      "add.cc.u32 %2, %2, u0;\n\t"
+      "addc.cc.u32 %3, %3, u1;\n\t"
+      "addc.u32 m, 0, 0;\n\t"
+      "sub.u32 m, 0, m;\n\t"
+      "add.cc.u32 %2, %2, m;\n\t"
+      "addc.u32 %3, %3, 0;\n\t"
+      // canonical: t >= p exactly when t + 2^32 - 1 carries
+      "add.cc.u32 q0, %2, 0xffffffff;\n\t"
+      "addc.cc.u32 q1, %3, 0;\n\t"
+      "addc.u32 %4, 0, 0;\n\t"
+      "mov.u32 %0, q0;\n\t"
+      "mov.u32 %1, q1;\n\t}"
+      : "=r"(r0), "=&r"(r1), "=&r"(t0), "=&r"(t1), "=r"(c)
+      : "r"((uint32_t)x), "r"((uint32_t)(x >> 32)), "r"((uint32_t)y), "r"((uint32_t)(y >> 32)),
+        "r"((uint32_t)z), "r"((uint32_t)(z >> 32)), "r"(0u), "r"((uint32_t)w), "r"((uint32_t)(w >> 32)));
+  return c ? gl_pack(r0, r1) : gl_pack(t0, t1);
 }
 
 __device__ __forceinline__ uint32_t bit_reverse(uint32_t x, uint32_t bits) {
@@ -221,6 +280,13 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass8(NttPass ps) {
     }
     __stcs(ps.dst + (g0 + c) * ps.out_c + (uint64_t)k * ps.out_k, v);
   }
+}
+
+// self-test hook: element-wise a op b (0 add, 1 sub, 2 mul)
+__global__ void k_gl_test(int op, const uint64_t *a, const uint64_t *b, uint64_t *out, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = op == 0 ? gl_add(a[i], b[i]) : op == 1 ? gl_sub(a[i], b[i]) : gl_mul(a[i], b[i]);
 }
 
 // Linear copy of n values in 16-byte vectors; the source may be host memory that the device
@@ -454,6 +520,29 @@ int ntt_evaluate(void *context, uint64_t *out, const uint64_t *in, uint64_t len)
   for (int k = 0; k < 4; k++) cudaEventElapsedTime(&ms[k], cx->ev[k], cx->ev[k + 1]);
   for (int k = 0; k < 4; k++) cx->last_ms[k] = ms[k];
   return 0;
+}
+
+int ntt_field_selftest(int32_t op, const uint64_t *a, const uint64_t *b, uint64_t *out, uint64_t n) {
+  g_err = 0;
+  if (n && (!a || !b || !out)) return fail(NTT_ERR_ARG, "ntt_field_selftest: null argument");
+  if (op < 0 || op > 2) return fail(NTT_ERR_ARG, "ntt_field_selftest: unknown operation %d", op);
+  if (n == 0) return 0;
+  const char *dev = getenv("MSM_DEVICE");
+  NCK(cudaSetDevice(dev ? atoi(dev) : 0));
+  uint64_t *d = nullptr;
+  NCK(cudaMalloc(&d, n * 24));
+  int rc = 0;
+  if (cudaMemcpy(d, a, n * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d + n, b, n * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = fail(NTT_ERR_CUDA, "ntt_field_selftest: upload failed");
+  if (!rc) {
+    k_gl_test<<<(unsigned)((n + 255) / 256), 256>>>(op, d, d + n, d + 2 * n, n);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(out, d + 2 * n, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(NTT_ERR_CUDA, "ntt_field_selftest: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  cudaFree(d);
+  return rc;
 }
 
 int ntt_last_timings(void *context, double *ms, int32_t max_stages) {

@@ -17,7 +17,7 @@ from . import MsmError, load_library
 
 GL_P = 0xFFFFFFFF00000001
 EXPORTED = ["ntt_init", "ntt_input_vector_size", "ntt_evaluate", "ntt_evaluate_device",
-            "ntt_last_timings", "ntt_last_error", "ntt_free"]
+            "ntt_last_timings", "ntt_last_error", "ntt_free", "ntt_field_selftest"]
 NTT_STAGES = ["h2d", "pass_a", "pass_b", "d2h"]
 
 _declared = False
@@ -36,6 +36,7 @@ def _lib():
             "ntt_last_timings": (ctypes.c_int, [P, ctypes.POINTER(ctypes.c_double), I32]),
             "ntt_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
             "ntt_free": (None, [P]),
+            "ntt_field_selftest": (ctypes.c_int, [I32, P, P, P, U64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -49,6 +50,16 @@ def last_error() -> str:
     buf = ctypes.create_string_buffer(512)
     code = _lib().ntt_last_error(buf, 512)
     return f"[{code}] {buf.value.decode(errors='replace')}"
+
+
+def field_selftest(op: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Element-wise a + b (op 0), a - b (1) or a b (2) modulo p on the GPU."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    out = np.empty_like(a)
+    if _lib().ntt_field_selftest(op, a.ctypes.data, b.ctypes.data, out.ctypes.data, a.size) != 0:
+        raise MsmError(f"ntt_field_selftest: {last_error()}")
+    return out
 
 
 class NttContext:

@@ -45,6 +45,10 @@ int ntt_evaluate_device(void *context, uint64_t *d_out, const uint64_t *d_in, vo
  * device-to-host copy.  Returns the number of values written. */
 int ntt_last_timings(void *context, double *ms, int32_t max_stages);
 
+/* Self-test hook: out[i] = a[i] op b[i] for op 0 (add), 1 (sub), 2 (mul) modulo p, inputs
+ * below p, on the GPU named by MSM_DEVICE. */
+int ntt_field_selftest(int32_t op, const uint64_t *a, const uint64_t *b, uint64_t *out, uint64_t n);
+
 /* Error code of the last failed call on this thread (0 if none) and its message. */
 int ntt_last_error(char *buf, size_t len);
 

@@ -30,6 +30,19 @@ def random_below_p(rng, n):
     return ((hi << np.uint64(32)) | lo) % np.uint64(P)
 
 
+def test_field_ops_on_edge_values(ntt_mod):
+    rng = np.random.default_rng(5)
+    edge = [0, 1, 2, P - 1, P - 2, 2**32 - 1, 2**32, 2**32 + 1, 2**63, P - 2**32, 2**64 - 2**33,
+            (P - 1) // 2, 0xFFFFFFFF00000000]
+    a = [x for x in edge for _ in edge] + [int(v) for v in random_below_p(rng, 20000)]
+    b = [y for _ in edge for y in edge] + [int(v) for v in random_below_p(rng, 20000)]
+    A, B = np.array(a, dtype=np.uint64), np.array(b, dtype=np.uint64)
+    for op, f in ((0, lambda x, y: (x + y) % P), (1, lambda x, y: (x - y) % P), (2, lambda x, y: x * y % P)):
+        got = ntt_mod.field_selftest(op, A, B)
+        for i in range(len(a)):
+            assert int(got[i]) == f(a[i], b[i]), (op, a[i], b[i])
+
+
 @pytest.mark.parametrize("log_n", [0, 1, 2, 3, 4, 7, 10, 12, 13, 15, 16, 18, 20, 21])
 def test_ntt_matches_oracle(ntt_mod, ocpu, log_n):
     rng = np.random.default_rng(100 + log_n)
