@@ -18,9 +18,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/ntt_gb300.h"
@@ -331,12 +334,20 @@ struct NttCtx {
   cudaEvent_t ev[5] = {};
   bool timing = false;
   double last_ms[4] = {0, 0, 0, 0};
+  // batches: a second input and output vector, and one stream each for uploads and downloads
+  uint64_t *d_in2 = nullptr, *d_out2 = nullptr;
+  cudaStream_t st_up = nullptr, st_down = nullptr;
+  cudaEvent_t up_done[2] = {}, comp_done[2] = {}, down_done[2] = {};
   ~NttCtx() {
-    for (uint64_t *p : {d_in, d_out, d_tmp, d_tw1, d_tw2, d_twlo, d_twhi})
+    for (uint64_t *p : {d_in, d_out, d_tmp, d_tw1, d_tw2, d_twlo, d_twhi, d_in2, d_out2})
       if (p) cudaFree(p);
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
-    if (st) cudaStreamDestroy(st);
+    for (int k = 0; k < 2; k++)
+      for (cudaEvent_t e : {up_done[k], comp_done[k], down_done[k]})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t x : {st, st_up, st_down})
+      if (x) cudaStreamDestroy(x);
   }
 };
 
@@ -542,6 +553,109 @@ int ntt_field_selftest(int32_t op, const uint64_t *a, const uint64_t *b, uint64_
       rc = fail(NTT_ERR_CUDA, "ntt_field_selftest: %s", cudaGetErrorString(cudaGetLastError()));
   }
   cudaFree(d);
+  return rc;
+}
+
+int ntt_evaluate_batch(void *context, uint64_t *out, const uint64_t *in, uint64_t count) {
+  g_err = 0;
+  auto *cx = (NttCtx *)context;
+  if (!cx || (count && (!out || !in))) return fail(NTT_ERR_ARG, "ntt_evaluate_batch: null argument");
+  if (count == 0) return 0;
+  NCK(cudaSetDevice(cx->device));
+  if (!cx->d_in2) {  // the second buffer pair and the copy streams, on first use
+    NCK(cudaMalloc(&cx->d_in2, cx->n * 8));
+    NCK(cudaMalloc(&cx->d_out2, cx->n * 8));
+    NCK(cudaStreamCreateWithFlags(&cx->st_up, cudaStreamNonBlocking));
+    NCK(cudaStreamCreateWithFlags(&cx->st_down, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) {
+      NCK(cudaEventCreateWithFlags(&cx->up_done[k], cudaEventDisableTiming));
+      NCK(cudaEventCreateWithFlags(&cx->comp_done[k], cudaEventDisableTiming));
+      NCK(cudaEventCreateWithFlags(&cx->down_done[k], cudaEventDisableTiming));
+    }
+  }
+  uint64_t *din[2] = {cx->d_in, cx->d_in2}, *dout[2] = {cx->d_out, cx->d_out2};
+  const size_t bytes = cx->n * 8;
+  // Uploads go through the driver; the copy kernel (NTT_BATCH_DIRECT=1) does not block this
+  // thread but competes with the transform for the SMs (2^24, 8 vectors: 1.57 against 1.37 ms
+  // per transform on GB300).
+  const char *bd = getenv("NTT_BATCH_DIRECT");
+  const bool direct_up = cx->host_direct && cx->n >= 2 && bd && strcmp(bd, "1") == 0;
+  const uint32_t cblocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)cx->num_sms * 8, cx->n / 512));
+  // A copy from or into pageable memory blocks its calling thread until it is done, so the
+  // downloads run on a worker thread while this thread uploads and enqueues transforms.
+  // Vector i uses slot i % 2.  Handshakes on the host: the worker takes vector i once its
+  // transform is enqueued (and its completion event recorded); this thread enqueues the
+  // transform of i + 2 only once the download of i is done, so no slot is overwritten while in
+  // use and no event is recorded again before the worker has waited on it.
+  std::mutex mu;
+  std::condition_variable cv;
+  uint64_t enqueued = 0, downloaded = 0;
+  int worker_rc = 0;
+  std::thread worker([&] {
+    cudaSetDevice(cx->device);
+    for (uint64_t i = 0; i < count; i++) {
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return enqueued > i || worker_rc < 0; });
+        if (worker_rc < 0) return;
+      }
+      const int k = (int)(i & 1);
+      cudaError_t e = cudaStreamWaitEvent(cx->st_down, cx->comp_done[k], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out + i * cx->n, dout[k], bytes, cudaMemcpyDeviceToHost, cx->st_down);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(cx->st_down);
+      std::lock_guard<std::mutex> lk(mu);
+      if (e != cudaSuccess) {
+        worker_rc = -1;
+        cv.notify_all();
+        return;
+      }
+      downloaded = i + 1;
+      cv.notify_all();
+    }
+  });
+  int rc = 0;
+  for (uint64_t i = 0; i < count && !rc; i++) {
+    const int k = (int)(i & 1);
+    if (i >= 2) {  // the download of i - 2 has emptied the output slot
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return downloaded >= i - 1 || worker_rc < 0; });
+      if (worker_rc < 0) break;
+    }
+    cudaError_t e = cudaSuccess;
+    if (i >= 2) e = cudaStreamWaitEvent(cx->st_up, cx->comp_done[k], 0);  // the input slot is free
+    if (e == cudaSuccess) {
+      const uint64_t *src = in + i * cx->n;
+      if (direct_up && ((uintptr_t)src & 15) == 0) {  // asynchronous: this thread does not block
+        k_ntt_copy<<<cblocks, 256, 0, cx->st_up>>>((const uint4 *)src, (uint4 *)din[k], cx->n / 2);
+        e = cudaGetLastError();
+      } else {
+        e = cudaMemcpyAsync(din[k], src, bytes, cudaMemcpyHostToDevice, cx->st_up);
+      }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(cx->up_done[k], cx->st_up);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cx->st, cx->up_done[k], 0);
+    if (e != cudaSuccess) {
+      rc = fail(NTT_ERR_CUDA, "ntt_evaluate_batch: %s", cudaGetErrorString(e));
+      break;
+    }
+    if ((rc = enqueue_ntt(cx, dout[k], din[k], cx->st, false))) break;
+    if ((e = cudaEventRecord(cx->comp_done[k], cx->st)) != cudaSuccess) {
+      rc = fail(NTT_ERR_CUDA, "ntt_evaluate_batch: %s", cudaGetErrorString(e));
+      break;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    enqueued = i + 1;
+    cv.notify_all();
+  }
+  if (rc) {
+    std::lock_guard<std::mutex> lk(mu);
+    worker_rc = -1;
+    cv.notify_all();
+  }
+  worker.join();
+  if (!rc && worker_rc < 0) rc = fail(NTT_ERR_CUDA, "ntt_evaluate_batch: a download failed");
+  cudaStreamSynchronize(cx->st);
   return rc;
 }
 

@@ -17,7 +17,8 @@ from . import MsmError, load_library
 
 GL_P = 0xFFFFFFFF00000001
 EXPORTED = ["ntt_init", "ntt_input_vector_size", "ntt_evaluate", "ntt_evaluate_device",
-            "ntt_last_timings", "ntt_last_error", "ntt_free", "ntt_field_selftest"]
+            "ntt_last_timings", "ntt_last_error", "ntt_free", "ntt_field_selftest",
+            "ntt_evaluate_batch"]
 NTT_STAGES = ["h2d", "pass_a", "pass_b", "d2h"]
 
 _declared = False
@@ -37,6 +38,7 @@ def _lib():
             "ntt_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
             "ntt_free": (None, [P]),
             "ntt_field_selftest": (ctypes.c_int, [I32, P, P, P, U64]),
+            "ntt_evaluate_batch": (ctypes.c_int, [P, P, P, U64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -84,6 +86,15 @@ class NttContext:
             out = np.empty_like(x)
         if _lib().ntt_evaluate(self.handle, out.ctypes.data, x.ctypes.data, self.n) != 0:
             raise MsmError(f"ntt_evaluate: {last_error()}")
+        return out
+
+    def evaluate_batch(self, values, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """NTTs of several vectors (rows of `values`), transfers overlapping the transforms."""
+        x = np.ascontiguousarray(values, dtype=np.uint64).reshape(-1, self.n)
+        if out is None:
+            out = np.empty_like(x)
+        if _lib().ntt_evaluate_batch(self.handle, out.ctypes.data, x.ctypes.data, x.shape[0]) != 0:
+            raise MsmError(f"ntt_evaluate_batch: {last_error()}")
         return out
 
     def evaluate_device(self, d_out: int, d_in: int, stream: int = 0) -> None:

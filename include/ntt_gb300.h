@@ -36,6 +36,13 @@ uint64_t ntt_input_vector_size(void *context);
  * negative error code. */
 int ntt_evaluate(void *context, uint64_t *out, const uint64_t *in, uint64_t len);
 
+/* `count` transforms back to back: out[i n ..] = NTT(in[i n ..]).  Two device vector pairs and
+ * three streams overlap the upload of vector i + 1 and the download of vector i - 1 with the
+ * transform of vector i, as the reference driver overlaps its user buffers
+ * (enqueue_evaluation_async / wait_for_result, driver.h:185-199; bench_throughput.cpp).  The
+ * second vector pair is allocated on the first call.  Synchronous. */
+int ntt_evaluate_batch(void *context, uint64_t *out, const uint64_t *in, uint64_t count);
+
 /* The same transform between device buffers, enqueued on `stream` (NULL: the context's own
  * stream); out must not alias in for transforms of at most 2^12 points.  No counterpart in the
  * reference (its buffers are the driver's). */
@@ -74,6 +81,10 @@ class NttGb300Driver {
   uint64_t input_vector_size() const { return ntt_input_vector_size(ctx_); }
   void simple_evaluate(uint64_t *output, const uint64_t *input, uint64_t data_length) {
     if (ntt_evaluate(ctx_, output, input, data_length) != 0) throw std::runtime_error(error());
+  }
+  /* count vectors of input_vector_size() elements, transfers overlapping the transforms */
+  void evaluate_batch(uint64_t *output, const uint64_t *input, uint64_t count) {
+    if (ntt_evaluate_batch(ctx_, output, input, count) != 0) throw std::runtime_error(error());
   }
 
  private:

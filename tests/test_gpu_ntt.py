@@ -124,3 +124,18 @@ def test_device_entry_point_and_roundtrip(ntt_mod, ocpu):
         assert np.array_equal(ocpu.ntt(got, inverse=True), x)  # the oracle's inverse undoes it
     finally:
         ctx.close()
+
+
+def test_batch_equals_single_calls(ntt_mod, ocpu):
+    rng = np.random.default_rng(17)
+    log_n = 18
+    xs = np.stack([random_below_p(rng, 1 << log_n) for _ in range(5)])
+    ctx = ntt_mod.NttContext(log_n)
+    try:
+        got = ctx.evaluate_batch(xs)
+        again = ctx.evaluate_batch(xs[:3])
+        for i in range(5):
+            assert np.array_equal(got[i], ocpu.ntt(xs[i])), i
+        assert np.array_equal(again, got[:3])
+    finally:
+        ctx.close()
