@@ -223,13 +223,24 @@ uint32_t whole_bucket_run(double mean) {
 // Longest run of entries one accumulate thread sums: whole buckets of `nwin_sharing` windows
 // but for the tail, and short enough that the n x nwin entries make at least ~2^17 runs: with
 // few, heavily loaded buckets (a fixed-base table of small width) whole-bucket runs would leave
-// most of the GPU idle.
+// most of the GPU idle.  A pass of at most 2^21 entries does not fill the GPU, and its time is
+// the longest run plus the merge of its split buckets: runs of about 2 sqrt(mean), at least 8,
+// balance the two.  Measured on GB300 (one MSM on width-16 tables, mean bucket load 8: 2^14
+// points): runs of 8 0.72 ms, 4 0.71 ms, 16 0.82 ms; at load 2 (2^12 points) runs of 2 to 32
+// are within 4% of each other, and at load 32 (2^16 points) 16 is best (1.06 ms, 8: 1.08 ms).
 uint32_t seg_len_for(uint64_t n, uint32_t nb, uint32_t nwin_sharing, uint32_t nwin) {
-  const uint32_t s = whole_bucket_run((double)n * nwin_sharing / std::max<uint32_t>(nb, 1));
+  const double mean = (double)n * nwin_sharing / std::max<uint32_t>(nb, 1);
+  const uint32_t s = whole_bucket_run(mean);
   const uint64_t entries = n * (uint64_t)nwin;
   uint32_t cap = 16;
   while (cap < 4096 && ((uint64_t)cap << 18) <= entries) cap <<= 1;  // entries / cap >= 2^17
-  return std::min(s, cap);
+  uint32_t r = std::min(s, cap);
+  if (entries <= (1ull << 21)) {
+    uint32_t t = 8;
+    while (t < 2.0 * std::sqrt(mean) && t < 4096) t <<= 1;
+    r = std::min(r, t);
+  }
+  return r;
 }
 
 Cfg heuristic_cfg(uint64_t n) {

@@ -848,24 +848,28 @@ constexpr uint32_t kAllLanes = 0xffffffffu;
 
 // Levels 2 and 3 are chains of dependent additions, so they run on quads: every quad of the
 // block executes every addition (a quad with nothing to add adds the identity), which keeps the
-// warps converged for the quad shuffles.
+// warps converged for the quad shuffles.  Blocks of NT threads (NT / 4 quads): with 128 each
+// SMSP runs one warp, so a step of the block's trees is shorter, but each quad sums twice as
+// many items in sequence as with 256.
 
-// Three independent sums over the block's quads at once (sh holds 3 x kRedQuads points): at
-// each tree level the 3 x stride additions are spread over the quads, so the three trees take 7
-// rounds of dependent additions instead of 18.  Only warps holding an active quad add (whole
-// warps, so their shuffles stay converged).  The sums are valid in quad 0.
+// Three independent sums over the block's quads at once (sh holds 3 x NT / 4 points): at each
+// tree level the 3 x stride additions are spread over the quads, so the three trees take
+// log2(NT / 4) + 1 rounds of dependent additions instead of 3 log2(NT / 4).  Only warps holding an
+// active quad add (whole warps, so their shuffles stay converged).  The sums are valid in quad 0.
+template <int NT>
 __device__ __forceinline__ void block_sum3(fq_t (&X)[3], uint4 *sh) {
+  constexpr uint32_t Q = NT / 4;
   const uint32_t q = threadIdx.x >> 2;
   const uint32_t warp_q0 = (threadIdx.x >> 5) * 8;  // first quad of this warp
-  for (int k = 0; k < 3; k++) dq_store(sh + (k * kRedQuads + q) * 12, X[k]);
+  for (int k = 0; k < 3; k++) dq_store(sh + (k * Q + q) * 12, X[k]);
   __syncthreads();
 #pragma unroll 1
-  for (uint32_t stride = kRedQuads / 2; stride > 0; stride >>= 1) {
+  for (uint32_t stride = Q / 2; stride > 0; stride >>= 1) {
 #pragma unroll 1
-    for (uint32_t u0 = 0; u0 < 3 * stride; u0 += kRedQuads) {
+    for (uint32_t u0 = 0; u0 < 3 * stride; u0 += Q) {
       const uint32_t u = u0 + q;  // item u: array u / stride, element u % stride
       const bool act = u < 3 * stride;
-      const uint32_t slot = act ? (u / stride) * kRedQuads + u % stride : 0;
+      const uint32_t slot = act ? (u / stride) * Q + u % stride : 0;
       fq_t a = dq_identity(), o = dq_identity();
       if (act) {
         a = dq_load(sh + slot * 12);
@@ -877,18 +881,20 @@ __device__ __forceinline__ void block_sum3(fq_t (&X)[3], uint4 *sh) {
       __syncthreads();
     }
   }
-  for (int k = 0; k < 3; k++) X[k] = dq_load(sh + k * kRedQuads * 12);
+  for (int k = 0; k < 3; k++) X[k] = dq_load(sh + k * Q * 12);
 }
 
 // Inclusive suffix sums over the quads: quad u gets sum_{v >= u} X_v (Hillis-Steele).
+template <int NT>
 __device__ __forceinline__ fq_t block_suffix_scan(fq_t X, uint4 *sh) {
+  constexpr uint32_t Q = NT / 4;
   const uint32_t q = threadIdx.x >> 2;
   dq_store(sh + q * 12, X);
   __syncthreads();
 #pragma unroll 1
-  for (uint32_t d = 1; d < kRedQuads; d <<= 1) {
+  for (uint32_t d = 1; d < Q; d <<= 1) {
     fq_t o = dq_identity();
-    if (q + d < kRedQuads) o = dq_load(sh + (q + d) * 12);
+    if (q + d < Q) o = dq_load(sh + (q + d) * 12);
     __syncthreads();
     X = dq_add(X, o, kAllLanes);
     dq_store(sh + q * 12, X);
@@ -903,11 +909,13 @@ __device__ __forceinline__ fq_t block_suffix_scan(fq_t X, uint4 *sh) {
 //   A = sum_u SA_u + 2^lin_log2 (sum_u T_u + per sum_u u RR_u),  R = sum_u RR_u,
 // where sum_u u RR_u = sum_{u >= 1} (suffix sum of RR at u): one block scan and three block
 // sums (run together), and only quad 0 doubles.
+template <int NT>
 __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log2, bool want_r,
                               uint4 *sh, fq_t &A_out, fq_t &R_out) {
+  constexpr uint32_t Q = NT / 4;
   const uint32_t q = threadIdx.x >> 2;
   uint32_t per = 1, per_log2 = 0;
-  while (per * kRedQuads < cnt) {
+  while (per * Q < cnt) {
     per <<= 1;
     per_log2++;
   }
@@ -925,10 +933,10 @@ __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log
     RR = dq_add(RR, R, kAllLanes);
     SA = dq_add(SA, A, kAllLanes);
   }
-  const fq_t suf = block_suffix_scan(RR, sh);
+  const fq_t suf = block_suffix_scan<NT>(RR, sh);
   if (want_r && q == 0) R_out = suf;  // suffix at 0 is the total
   fq_t S[3] = {q ? suf : dq_identity(), T, SA};
-  block_sum3(S, sh);
+  block_sum3<NT>(S, sh);
   if (q == 0) {  // lanes 0..3 of warp 0
     fq_t X = S[0];
 #pragma unroll 1
@@ -940,17 +948,19 @@ __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log
   }
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_reduce2(PassBuffers pb) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_reduce2(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t g = blockIdx.x;
   if (g >= pb.n_grps) return;
-  __shared__ uint4 sh[3 * kRedQuads * 12];
+  __shared__ uint4 sh[3 * (NT / 4) * 12];
   const WinDesc wd = pb.wins[find_win_grp(pb.wins, pb.n_wins, g)];
   const uint32_t G = 1u << pb.grp_len_log2;
   const uint32_t first = (g - wd.grp_begin) * G;
   const uint32_t cnt = min(G, wd.nseg - first);
   fq_t A, R;
-  block_combine(pb.seg_out + (size_t)(wd.seg_begin + first) * 24, cnt, pb.red_len_log2, true, sh, A, R);
+  block_combine<NT>(pb.seg_out + (size_t)(wd.seg_begin + first) * 24, cnt, pb.red_len_log2, true,
+                    sh, A, R);
   if (threadIdx.x < 4) {  // quad 0: one coordinate per lane
     dq_store(pb.grp_out + (size_t)g * 24, R);
     dq_store(pb.grp_out + (size_t)g * 24 + 12, A);
@@ -996,16 +1006,17 @@ __global__ void __launch_bounds__(128) k_reduce3_small(PassBuffers pb) {
   dq_store(pb.win_sum + (size_t)gw * 12, out);
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_reduce3(PassBuffers pb) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_reduce3(PassBuffers pb) {
   if (pb.counters[CNT_ERROR]) return;
   const uint32_t gw = blockIdx.x;
   if (gw >= pb.n_wins) return;
-  __shared__ uint4 sh[3 * kRedQuads * 12];
+  __shared__ uint4 sh[3 * (NT / 4) * 12];
   const WinDesc wd = pb.wins[gw];
   if (wd.ngrp <= kRed3SmallMax) return;  // k_reduce3_small's
   fq_t A, R;
-  block_combine(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp, pb.red_len_log2 + pb.grp_len_log2,
-                false, sh, A, R);
+  block_combine<NT>(pb.grp_out + (size_t)wd.grp_begin * 24, wd.ngrp,
+                    pb.red_len_log2 + pb.grp_len_log2, false, sh, A, R);
   if (threadIdx.x < 4) dq_store(pb.win_sum + (size_t)gw * 12, A);
 }
 
@@ -1242,15 +1253,23 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
     launched++;
   }
   mark(7);
+  // Level 2 in blocks of 256 threads; level 3 (one block per window) in blocks of 128 while
+  // they fit on the SMs in one wave.  Measured on GB300 (ms, 256 against 128 threads): level 3
+  // of one fixed-base MSM of 2^12 / 2^16 / 2^20 / 2^24 points 0.130 / 0.145 / 0.171 / 0.215
+  // against 0.107 / 0.123 / 0.154 / 0.206; level 2, groups of 512 runs at 2^20 / 2^24,
+  // 0.188 / 0.268 against 0.214 / 0.348 (each quad then sums twice as many runs in sequence).
   if (pb.n_grps > 0) {
-    k_reduce2<<<pb.n_grps, kRedThreads, 0, st>>>(pb);
+    k_reduce2<256><<<pb.n_grps, 256, 0, st>>>(pb);
     launched++;
   }
   mark(8);
   if (pb.n_wins > 0) {
     k_reduce3_small<<<(pb.n_wins + 31) / 32, 128, 0, st>>>(pb);
     launched++;
-    k_reduce3<<<pb.n_wins, kRedThreads, 0, st>>>(pb);
+    if (pb.n_wins <= (uint32_t)num_sms)
+      k_reduce3<128><<<pb.n_wins, 128, 0, st>>>(pb);
+    else
+      k_reduce3<256><<<pb.n_wins, 256, 0, st>>>(pb);
     launched++;
   }
   mark(9);

@@ -198,7 +198,9 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
 // bank conflicts for m = 4096.
 __device__ __forceinline__ uint32_t slot(uint32_t q) { return q ^ ((q >> 4) & 15u) ^ ((q >> 8) & 15u); }
 
-template <int R>
+// LAST: the round ending at half size 1, where every unit has j = 0 and the twiddle of a pair
+// whose position within the half is 0 is 1 (7 of the 12 of a radix-8 round): no product there.
+template <int R, bool LAST>
 __device__ __forceinline__ void dif_unit(uint64_t (&x)[8], uint32_t j, uint32_t log_hmin,
                                          uint32_t log_m, const uint64_t *tw) {
 #pragma unroll
@@ -208,18 +210,22 @@ __device__ __forceinline__ void dif_unit(uint64_t (&x)[8], uint32_t j, uint32_t 
 #pragma unroll
     for (int t = 0; t < (1 << R); t++) {
       if (t & d) continue;
-      const uint32_t jp = j + ((uint32_t)(t & (d - 1)) << log_hmin);  // position within the half
-      const uint64_t w = tw[jp << (log_m - 1 - log_h)];              // w_2H^jp = w_m^(jp m / 2H)
       const uint64_t u = x[t], v = x[t + d];
       x[t] = gl_add(u, v);
-      x[t + d] = gl_mul(gl_sub(u, v), w);
+      if (LAST && (t & (d - 1)) == 0) {
+        x[t + d] = gl_sub(u, v);
+      } else {
+        const uint32_t jp = j + ((uint32_t)(t & (d - 1)) << log_hmin);  // position within the half
+        const uint64_t w = tw[jp << (log_m - 1 - log_h)];              // w_2H^jp = w_m^(jp m / 2H)
+        x[t + d] = gl_mul(gl_sub(u, v), w);
+      }
     }
   }
 }
 
 // One round of R stages over every unit of the block's transforms; the first round reads the
 // transforms from global memory (natural order), the others from shared memory.
-template <int R>
+template <int R, bool LAST>
 __device__ __forceinline__ void dif_round(const NttPass &ps, uint64_t *sm, uint32_t pitch,
                                           const uint64_t *tw, uint32_t log_hmin, bool from_global) {
   const uint32_t m = 1u << ps.log_m, C = ps.cols, units = m >> R;
@@ -241,7 +247,7 @@ __device__ __forceinline__ void dif_round(const NttPass &ps, uint64_t *sm, uint3
         x[t] = a[slot(q)];
       }
     }
-    dif_unit<R>(x, j, log_hmin, ps.log_m, tw);
+    dif_unit<R, LAST>(x, j, log_hmin, ps.log_m, tw);
 #pragma unroll
     for (int t = 0; t < (1 << R); t++) a[slot(q0 + ((uint32_t)t << log_hmin))] = x[t];
   }
@@ -259,9 +265,15 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass8(NttPass ps) {
   while (log_h0 >= 0) {
     const int r = log_h0 + 1 >= 3 ? 3 : log_h0 + 1;
     const uint32_t log_hmin = (uint32_t)(log_h0 - (r - 1));
-    if (r == 3) dif_round<3>(ps, sm, pitch, tw, log_hmin, first);
-    else if (r == 2) dif_round<2>(ps, sm, pitch, tw, log_hmin, first);
-    else dif_round<1>(ps, sm, pitch, tw, log_hmin, first);
+    if (log_hmin == 0) {  // the last round
+      if (r == 3) dif_round<3, true>(ps, sm, pitch, tw, 0, first);
+      else if (r == 2) dif_round<2, true>(ps, sm, pitch, tw, 0, first);
+      else dif_round<1, true>(ps, sm, pitch, tw, 0, first);
+    } else {
+      if (r == 3) dif_round<3, false>(ps, sm, pitch, tw, log_hmin, first);
+      else if (r == 2) dif_round<2, false>(ps, sm, pitch, tw, log_hmin, first);
+      else dif_round<1, false>(ps, sm, pitch, tw, log_hmin, first);
+    }
     __syncthreads();
     first = false;
     log_h0 -= r;
