@@ -168,6 +168,14 @@ def cpu_msm_time(points, scalars, threads):
     return time.perf_counter() - t0, out
 
 
+def workload_config(log2n):
+    """The config both arms report for the plain workload (one MSM of 2^log2n points)."""
+    n = 1 << log2n
+    return {"workload": f"plain single MSM, BLS12-377 G1, N=2^{log2n}", "n": n,
+            "l2": f"inputs larger than L2: {n * 32 / 2**20:.0f} MB of scalars and at least "
+                  f"{n * 144 / 2**20:.0f} MB of resident base records per MSM; no L2 flush"}
+
+
 def run_reference(args, rank, world):
     """Reference arm: the CPU port of the oracle algorithm on all host cores."""
     if rank != 0:
@@ -190,7 +198,7 @@ def run_reference(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
-        "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n},
+        "config": workload_config(args.log2n),
         "cpu_baseline": {"value": v, "unit": "MSM/s", "cores": cores, "kind": "port",
                          "sample": f"one full MSM of 2^{args.log2n} points per timed step; "
                                    f"warm-up steps on the first {nw} points"},
@@ -295,8 +303,9 @@ def run_ours(args, rank, world, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded k_i*G bases, uniform 253-bit scalars)",
-        "config": {"workload": f"plain single MSM, BLS12-377 G1, N=2^{args.log2n}", "n": n,
-                   "l2": f"inputs larger than L2 ({n * 32 / 2**20:.0f} MB scalars, "
+        # both arms carry the same config; the layout this pass ran is beside it
+        "config": workload_config(args.log2n),
+        "layout": {"l2": f"inputs larger than L2 ({n * 32 / 2**20:.0f} MB scalars, "
                          f"{ctx_info['resident_bytes'] / 2**30:.1f} GB of resident base records: "
                          + (f"fixed-base tables of width {ctx_info['table_bits']} "
                             f"({ctx_info['table_windows']} records per base)"
