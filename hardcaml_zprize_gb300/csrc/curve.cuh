@@ -104,6 +104,34 @@ static __device__ __noinline__ xyzt_t te_dbl_ool(const xyzt_t &p) { return te_db
 static __device__ __noinline__ fq_t fq_mul_ool(const fq_t &a, const fq_t &b) { return fq_mul(a, b); }
 static __device__ __noinline__ fq_t fq_sqr_ool(const fq_t &a) { return fq_mul(a, a); }
 
+// p + q by the dedicated addition, add-2008-hwcd-4 with a = -1: 8 products, no multiple of d.
+//   A = (Y1 - X1)(Y2 + X2), B = (Y1 + X1)(Y2 - X2), C = 2 Z1 T2, D = 2 T1 Z2,
+//   E = D + C, F = B - A, G = B + A, H = D - C;  X3 = E F, Y3 = G H, T3 = E H, Z3 = F G.
+// In affine terms x3 = E / G = (x1 y1 + x2 y2) / (y1 y2 - x1 x2) and y3 = H / F =
+// (x1 y1 - x2 y2) / (x1 y2 - y1 x2), the twisted-Edwards sum wherever F G != 0.  This formula and
+// the unified one are polynomial maps that agree on a dense set of pairs, so their 2 x 2 minors
+// vanish everywhere: wherever F G != 0 the result is the unified formula's point.  F G = 0
+// (doubling, the identity plus a point with T = 0, ...) is tested right after the first two
+// products, and the unified formula (9 products) is used then.  E and H feed products only, so
+// they stay unreduced (below 4q).
+__device__ __forceinline__ xyzt_t te_add_fast(const xyzt_t &p, const xyzt_t &q) {
+  const fq_t A = fq_mul_nv(fq_sub_lazy(p.y, p.x), fq_add_lazy(q.y, q.x));
+  const fq_t B = fq_mul_nv(fq_add_lazy(p.y, p.x), fq_sub_lazy(q.y, q.x));
+  const fq_t F = fq_sub(B, A);
+  const fq_t G = fq_add(B, A);
+  if (fq_is_zero(F) || fq_is_zero(G)) return te_add_ool(p, q);
+  const fq_t C = fq_dbl(fq_mul_nv(p.z, q.t));
+  const fq_t D = fq_dbl(fq_mul_nv(p.t, q.z));
+  const fq_t E = fq_add_lazy(D, C);
+  const fq_t H = fq_sub_lazy(D, C);
+  xyzt_t r;
+  r.x = fq_mul_nv(E, F);
+  r.y = fq_mul_nv(G, H);
+  r.t = fq_mul_nv(E, H);
+  r.z = fq_mul_nv(F, G);
+  return r;
+}
+
 // small scalar multiple k*p (k >= 0) by double-and-add from the top bit
 static __device__ __noinline__ xyzt_t te_mul_small(const xyzt_t &p, uint32_t k) {
   xyzt_t r = xyzt_identity();

@@ -752,18 +752,30 @@ __global__ void __launch_bounds__(128) k_reduce1(PassBuffers pb) {
   const uint32_t hi = min(lo + L, wd.nb);
   xyzt_t R = xyzt_identity(), A = xyzt_identity();
   bool r_live = false, a_live = false;
+  bool a_is_r = false;  // A was set to R at the first live bucket and R has not changed since
 #pragma unroll 1
   for (uint32_t b = hi; b-- > lo;) {
     const uint32_t gb = wd.bucket_begin + b;
     if (pb.count[gb] != 0) {
       xyzt_t B;
       xyzt_load(B, pb.partials + (size_t)pb.taskoff[gb] * 12);
-      R = r_live ? te_add(R, B) : B;
+      R = r_live ? te_add_fast(R, B) : B;
       r_live = true;
+      a_is_r = false;
     }
     if (r_live) {
-      A = a_live ? te_add(A, R) : R;
-      a_live = true;
+      if (!a_live) {
+        A = R;
+        a_live = true;
+        a_is_r = true;
+      } else {
+        // with A = R (an empty bucket right after the first live one) A + R is a doubling, the
+        // dedicated formula's failure; a warp holding such a lane takes the unified formula for
+        // this step instead of running both
+        if (__any_sync(__activemask(), a_is_r)) A = te_add(A, R);
+        else A = te_add_fast(A, R);
+        a_is_r = false;
+      }
     }
   }
   xyzt_store(pb.seg_out + (size_t)s * 24, R);
@@ -820,8 +832,8 @@ static __device__ __noinline__ fq_t dq_dbl(fq_t p, uint32_t mask) {
   return fq_mul(pick4(l, E, E, G, F), pick4(l, F, H, H, G));
 }
 
-// add-2008-hwcd-3 with k = 2d (the same formula as te_add)
-static __device__ __noinline__ fq_t dq_add(fq_t p, fq_t q, uint32_t mask) {
+// add-2008-hwcd-3 with k = 2d (the same formula as te_add): three product latencies
+static __device__ __noinline__ fq_t dq_add_unified(fq_t p, fq_t q, uint32_t mask) {
   const uint32_t kc[FQ_LIMBS] = BLS_TE_K;
   const int l = dq_lane();
   const fq_t po = dq_xchg(p, 2, mask), qo = dq_xchg(q, 2, mask);  // lanes 0, 2 swap X and Y
@@ -840,6 +852,48 @@ static __device__ __noinline__ fq_t dq_add(fq_t p, fq_t q, uint32_t mask) {
   const fq_t w3 = dq_xchg(w, 3, mask);  // lane 1 gets H, lane 2 gets G
   // X3 = E F (lane 0), T3 = E H (lane 1), Y3 = G H (lane 2), Z3 = F G (lane 3)
   return fq_mul(pick4(l, u, u1, w3, u), pick4(l, u1, w3, w, w));
+}
+
+// this lane's coordinate equals the identity's as dq_identity() writes it, on all four lanes
+__device__ __forceinline__ bool dq_is_identity_bits(const fq_t &p, uint32_t mask) {
+  const uint32_t one[FQ_LIMBS] = BLS_ONE;
+  const bool unit = dq_lane() >= 2;  // Y and Z are one, X and T zero
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < FQ_LIMBS; j++) acc |= p.v[j] ^ (unit ? one[j] : 0u);
+  int ok = acc == 0;
+  ok &= __shfl_xor_sync(mask, ok, 1, 4);
+  ok &= __shfl_xor_sync(mask, ok, 2, 4);
+  return ok != 0;
+}
+
+// p + q by the dedicated formula (curve.cuh te_add_fast): two product latencies instead of three.
+//   lane 0: A = (Y1 - X1)(Y2 + X2), lane 2: B = (Y1 + X1)(Y2 - X2), lane 1: C = 2 Z1 T2,
+//   lane 3: D = 2 T1 Z2; then X3 = E F (lane 0), T3 = E H (1), Y3 = G H (2), Z3 = F G (3).
+// Where it gives Z3 = 0 the quad takes the unified formula; an operand that is the identity as
+// dq_identity() writes it (padding, empty runs) returns the other one unchanged.  Every lane of
+// `mask` calls this, and the branch to the unified formula is uniform over `mask`.
+static __device__ __noinline__ fq_t dq_add(fq_t p, fq_t q, uint32_t mask) {
+  const int l = dq_lane();
+  const bool pid = dq_is_identity_bits(p, mask), qid = dq_is_identity_bits(q, mask);
+  const fq_t po = dq_xchg(p, 2, mask), qo = dq_xchg(q, 2, mask);  // X <-> Y on 0, 2; T <-> Z on 1, 3
+  const fq_t m1 = l == 0 ? fq_sub_lazy(po, p) : l == 2 ? fq_add_lazy(p, po) : po;
+  const fq_t m2 = l == 0 ? fq_add_lazy(qo, q) : l == 2 ? fq_sub_lazy(q, qo) : q;
+  fq_t pr = fq_mul(m1, m2);  // A, C' = Z1 T2, B, D' = T1 Z2 on lanes 0..3
+  if (l & 1) pr = fq_dbl(pr);
+  // pairs {0, 2}: F = B - A, G = B + A; pairs {1, 3}: H = D - C, E = D + C
+  const fq_t o = dq_xchg(pr, 2, mask);
+  const fq_t lo = l < 2 ? pr : o, hi = l < 2 ? o : pr;
+  const fq_t u = fq_sub_lazy(hi, lo), w = fq_add_lazy(hi, lo);
+  const fq_t u1 = dq_xchg(u, 1, mask), w1 = dq_xchg(w, 1, mask);
+  fq_t r = fq_mul(pick4(l, w1, w, w, u1), pick4(l, u, u, u1, w1));
+  const int zero = fq_is_zero(r);
+  const bool need = __shfl_sync(mask, zero, 3, 4) != 0 && !pid && !qid;  // Z3 = 0 on lane 3
+  if (__any_sync(mask, need)) {
+    const fq_t ru = dq_add_unified(p, q, mask);
+    if (need) r = ru;
+  }
+  return pid ? q : qid ? p : r;
 }
 
 constexpr int kRedThreads = 256;
