@@ -86,48 +86,41 @@ __device__ __forceinline__ uint64_t gl_sub(uint64_t a, uint64_t b) {
   return gl_pack(d0, d1);
 }
 
-// a b: the 128-bit product (r3 r2 r1 r0) from four wide multiplies, then
-// lo - hh + hl (2^32 - 1) with lo = r1 r0, hl = r2, hh = r3 (2^64 = 2^32 - 1, 2^96 = -1), each
-// step corrected by its own carry or borrow, and a last conditional subtraction of p
+// a b: the 128-bit product (r3 r2 r1 r0) from four wide multiplies whose 64-bit addends carry
+// the partial products' overflow (the carries ride in the multiplies, which run on the multiply
+// pipe; the passes are bound by the integer ALU pipe), then lo + hl (2^32 - 1) - hh with
+// lo = r1 r0, hl = r2, hh = r3 (2^64 = 2^32 - 1, 2^96 = -1 mod p): hl (2^32 - 1) is a fifth wide
+// multiply, each step is corrected by its own carry or borrow, and a last conditional
+// subtraction of p makes the value canonical.
+//   s = lo + hl (2^32 - 1) < 2^65; a carry out adds 2^32 - 1, and then s < 2^64 - 2^32;
+//   t = s - hh; a borrow subtracts 2^32 - 1 more (t + p), which stays above zero.
 __device__ __forceinline__ uint64_t gl_mul(uint64_t a, uint64_t b) {
   const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
-  const uint64_t x = (uint64_t)a0 * b0, y = (uint64_t)a0 * b1, z = (uint64_t)a1 * b0,
-                 w = (uint64_t)a1 * b1;
-  uint32_t r0, r1, t0, t1, c;
-  asm("{\n\t.reg .u32 r2, r3, m, u0, u1, q0, q1;\n\t"
-      // r1 r2 r3 = x.hi + y + z 2^0 + w 2^32 aligned: (r3 r2 r1 r0) = x + (y + z) 2^32 + w 2^64
-      "add.cc.u32 %1, %6, %7;\n\t"        // r1 = x.hi + y.lo
-      "addc.cc.u32 r2, %12, %8;\n\t"      // r2 = w.lo + y.hi
-      "addc.u32 r3, %13, 0;\n\t"          // r3 = w.hi
-      "add.cc.u32 %1, %1, %9;\n\t"        // r1 += z.lo
-      "addc.cc.u32 r2, r2, %10;\n\t"      // r2 += z.hi
-      "addc.u32 r3, r3, 0;\n\t"
-      // t = lo - hh, on a borrow subtract 2^32 - 1 more
-      "sub.cc.u32 %2, %5, r3;\n\t"
-      "subc.cc.u32 %3, %1, 0;\n\t"
-      "subc.u32 m, 0, 0;\n\t"
-      "sub.cc.u32 %2, %2, m;\n\t"
-      "subc.u32 %3, %3, 0;\n\t"
-      // u = hl (2^32 - 1) = hl 2^32 - hl
-      "sub.cc.u32 u0, 0, r2;\n\t"
-      "subc.u32 u1, r2, 0;\n\t"
-      // t += u, on a carry add 2^32 - 1
-      "add.cc.u32 %2, %2, u0;\n\t"
-      "addc.cc.u32 %3, %3, u1;\n\t"
+  const uint64_t x = (uint64_t)a0 * b0;
+  const uint64_t y = (uint64_t)a0 * b1 + (x >> 32);
+  const uint64_t z = (uint64_t)a1 * b0 + (uint32_t)y;
+  const uint64_t w = (uint64_t)a1 * b1 + (y >> 32) + (z >> 32);
+  const uint64_t u = (uint64_t)(uint32_t)w * 0xffffffffu;  // hl (2^32 - 1)
+  uint32_t t0, t1, q0, q1, c;
+  asm("{\n\t.reg .u32 m;\n\t"
+      "add.cc.u32 %0, %5, %7;\n\t"       // s = lo + u
+      "addc.cc.u32 %1, %6, %8;\n\t"
       "addc.u32 m, 0, 0;\n\t"
-      "sub.u32 m, 0, m;\n\t"
-      "add.cc.u32 %2, %2, m;\n\t"
-      "addc.u32 %3, %3, 0;\n\t"
-      // canonical: t >= p exactly when t + 2^32 - 1 carries
-      "add.cc.u32 q0, %2, 0xffffffff;\n\t"
-      "addc.cc.u32 q1, %3, 0;\n\t"
-      "addc.u32 %4, 0, 0;\n\t"
-      "mov.u32 %0, q0;\n\t"
-      "mov.u32 %1, q1;\n\t}"
-      : "=r"(r0), "=&r"(r1), "=&r"(t0), "=&r"(t1), "=r"(c)
-      : "r"((uint32_t)x), "r"((uint32_t)(x >> 32)), "r"((uint32_t)y), "r"((uint32_t)(y >> 32)),
-        "r"((uint32_t)z), "r"((uint32_t)(z >> 32)), "r"(0u), "r"((uint32_t)w), "r"((uint32_t)(w >> 32)));
-  return c ? gl_pack(r0, r1) : gl_pack(t0, t1);
+      "neg.s32 m, m;\n\t"                // 2^32 - 1 on a carry
+      "add.cc.u32 %0, %0, m;\n\t"
+      "addc.u32 %1, %1, 0;\n\t"
+      "sub.cc.u32 %0, %0, %9;\n\t"       // t = s - hh
+      "subc.cc.u32 %1, %1, 0;\n\t"
+      "subc.u32 m, 0, 0;\n\t"            // 2^32 - 1 on a borrow
+      "sub.cc.u32 %0, %0, m;\n\t"
+      "subc.u32 %1, %1, 0;\n\t"
+      "add.cc.u32 %2, %0, 0xffffffff;\n\t"  // t >= p exactly when t + 2^32 - 1 carries
+      "addc.cc.u32 %3, %1, 0;\n\t"
+      "addc.u32 %4, 0, 0;\n\t}"
+      : "=&r"(t0), "=&r"(t1), "=&r"(q0), "=&r"(q1), "=&r"(c)
+      : "r"((uint32_t)x), "r"((uint32_t)z), "r"((uint32_t)u), "r"((uint32_t)(u >> 32)),
+        "r"((uint32_t)(w >> 32)));
+  return c ? gl_pack(q0, q1) : gl_pack(t0, t1);
 }
 
 __device__ __forceinline__ uint32_t bit_reverse(uint32_t x, uint32_t bits) {
