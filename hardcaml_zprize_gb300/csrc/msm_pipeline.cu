@@ -605,6 +605,20 @@ __device__ __forceinline__ xyzt_t te_madd_staged(const xyzt_t &p, const uint4 *s
   return r;
 }
 
+// The first entry of a run starts the sum from the base itself instead of adding it to the
+// identity: x = (y+x)/2 - (y-x)/2, y = (y+x)/2 + (y-x)/2 (x negated for a negative digit), z = 1,
+// t = x y -- one product instead of seven.  The lanes of a warp take their runs together and the
+// runs are nearly equal in length (longest first), so the branch is the same on every lane.
+__device__ __forceinline__ xyzt_t te_from_staged(const uint4 *sh, bool neg) {
+  const fq_t ymx = staged_fq(sh, 0), ypx = staged_fq(sh, 1);
+  xyzt_t r;
+  r.x = neg ? fq_sub(ymx, ypx) : fq_sub(ypx, ymx);
+  r.y = fq_add(ypx, ymx);
+  r.z = fq_one();
+  r.t = fq_mul_nv(r.x, r.y);
+  return r;
+}
+
 __global__ void __launch_bounds__(128, 4) k_accumulate(PassBuffers pb) {
   __shared__ uint4 sh[9 * 128];
   const int lane = threadIdx.x & 31;
@@ -630,7 +644,9 @@ __global__ void __launch_bounds__(128, 4) k_accumulate(PassBuffers pb) {
         const uint4 *src = pb.bases + (size_t)idx * 9;
 #pragma unroll
         for (int k = 0; k < 9; k++) sh[k * 128 + threadIdx.x] = src[k];
-        acc = te_madd_staged(acc, sh, (v >> 31) != 0);
+        const bool neg = (v >> 31) != 0;
+        if (e == 0) acc = te_from_staged(sh, neg);
+        else acc = te_madd_staged(acc, sh, neg);
       }
       xyzt_store(pb.partials + (size_t)t * 12, acc);
     }
