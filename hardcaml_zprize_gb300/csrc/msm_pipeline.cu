@@ -990,9 +990,14 @@ __device__ void block_combine(const uint4 *items, uint32_t cnt, uint32_t lin_log
     per_log2++;
   }
   const uint32_t i0 = q * per;
+  // the last run of the quad's share starts the sums (T = 0 R, RR = R, SA = A: no additions)
   fq_t SA = dq_identity(), T = dq_identity(), RR = dq_identity();
+  if (i0 + per - 1 < cnt) {  // runs past cnt are the identity
+    RR = dq_load(items + (size_t)(i0 + per - 1) * 24);
+    SA = dq_load(items + (size_t)(i0 + per - 1) * 24 + 12);
+  }
 #pragma unroll 1
-  for (uint32_t k = per; k-- > 0;) {  // runs past cnt are the identity
+  for (uint32_t k = per - 1; k-- > 0;) {
     const uint32_t i = i0 + k;
     T = dq_add(T, RR, kAllLanes);
     fq_t R = dq_identity(), A = dq_identity();
