@@ -38,8 +38,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+C_MUL = 588     # one Montgomery product: 12 x 12 limb products, lo and hi, plus the reduction
 C_MADD = 4116   # 7 Montgomery products x 588 IMAD (12 x 32-bit limbs)
 C_ADD = 5292    # 9 products
+
+
+def accumulate_imad(stats):
+    """IMAD (588 per product) that k_accumulate executes in one pass: every run (task) starts
+    from its first base with one product, and each further entry is a 7-product mixed add.  The
+    survey's convention credits one mixed add per sorted entry (entries x 4116), which counts
+    6 products per run that the kernel does not do."""
+    entries, tasks = int(stats["entries"]), int(stats["tasks"])
+    return (entries - tasks) * C_MADD + tasks * C_MUL
 
 
 def hbm_view(achieved_bytes_per_s):
@@ -288,7 +298,7 @@ def run_ours(args, rank, world, local):
     msm_s = t_dev / args.steps
     t_acc = stage_acc.get("accumulate", 0) * 1e-3
     entries = int(stats["entries"])  # mixed adds of one pass: its nonzero digits
-    acc_imad = entries * C_MADD
+    acc_imad = accumulate_imad(stats)
     achieved = acc_imad / t_acc if t_acc > 0 else None
     traffic = None
     tf = os.path.join(ROOT, "profiles", "k_accumulate_traffic.json")
@@ -327,8 +337,12 @@ def run_ours(args, rank, world, local):
             "unit": "TIMAD/s", "frac": (achieved / peak_imad) if achieved else None,
             "traffic": traffic,
             "algorithmic_imad_per_launch": acc_imad, "entries_per_launch": entries,
+            "runs_per_launch": int(stats["tasks"]),
+            "imad_convention_one_madd_per_entry": entries * C_MADD,
             "peak_source": "measured in this run: independent mad.lo chains on all SMs "
-                           "(msm_measure_int_peaks); algorithmic count 588 IMAD per 12-limb product",
+                           "(msm_measure_int_peaks); algorithmic count 588 IMAD per 12-limb "
+                           "product, 7 products per mixed add after each run's first entry "
+                           "(1 product)",
             "peak_mad_lo_hi_pairs": peaks["mad_lo_hi"] / 1e12, "peak_mad_hi": peaks["mad_hi"] / 1e12,
             "frac_vs_lo_hi_pairs": (achieved / peaks["mad_lo_hi"]) if achieved else None,
             # A(N) counts a windowed signed Pippenger (c in 10..16); the pass runs on fixed-base
@@ -424,7 +438,7 @@ def bench_plain_form(args, eng, torch, dev, pts, dev_sc, last_sc, out_cpu, peak_
         ctx.set_timing(False)
         got = ctx.mult(last_sc)[0]
         t_acc = stages.get("accumulate", 0) * 1e-3
-        acc_imad = int(stats["entries"]) * C_MADD
+        acc_imad = accumulate_imad(stats)
         return {
             "workload": f"plain single MSM, N=2^{args.log2n}, windowed signed digits over 144 B records",
             "resident_bytes": info["resident_bytes"], "window_bits": cfg["window_bits"],
@@ -527,10 +541,11 @@ def fixed_base_large(args, eng, peaks, local, log2n, check=True):
         "h2d_bytes_per_batch": n * 32, "d2h_bytes_per_batch": 144,
         "stages_ms": stages, "pass_stats": stats,
         "hbm_gbs_base_and_scalar_streams": (entries * 148 + n * 32) / t_acc / 1e9 if t_acc else None,
-        "imad": {"kernel": "k_accumulate", "achieved_tera": entries * C_MADD / t_acc / 1e12 if t_acc else None,
+        "imad": {"kernel": "k_accumulate",
+                 "achieved_tera": accumulate_imad(stats) / t_acc / 1e12 if t_acc else None,
                  "peak_mad_lo_tera": peaks["mad_lo"] / 1e12,
-                 "frac": (entries * C_MADD / t_acc / peaks["mad_lo"]) if t_acc else None,
-                 "entries_per_msm": entries},
+                 "frac": (accumulate_imad(stats) / t_acc / peaks["mad_lo"]) if t_acc else None,
+                 "entries_per_msm": entries, "runs_per_msm": int(stats["tasks"])},
         "parity": parity, "clocks": clk.summary(),
         "setup_s": {"generate_bases": t_gen, "msm_init_with_tables": t_init},
         "reference_fpga": {"total_s": 20.336, "msm_per_s": 4 / 20.336,
@@ -839,10 +854,16 @@ def bench_served(args, eng, ctx, n):
     nbase = min(n, 1 << 22)
     m = args.served_requests
     rng, sizes, offs, reqs = served_mix(args.seed, eng.generate_scalars, m, nbase)
-    # plain: one request at a time
-    t0 = time.perf_counter()
-    plain_out = [ctx.mult_uneven([s], [o], r)[0] for s, o, r in zip(sizes, offs, reqs)]
-    t_plain = time.perf_counter() - t0
+    # plain: one request at a time, after an untimed pass of the largest request (the workspace
+    # then holds every size), best of two rounds; the served loads below are multiples of it
+    big = max(range(m), key=lambda j: sizes[j])
+    ctx.mult_uneven([sizes[big]], [offs[big]], reqs[big])
+    t_plain = None
+    for _ in range(2):
+        t0 = time.perf_counter()
+        plain_out = [ctx.mult_uneven([s], [o], r)[0] for s, o, r in zip(sizes, offs, reqs)]
+        t = time.perf_counter() - t0
+        t_plain = t if t_plain is None else min(t_plain, t)
     plain_rate = m / t_plain
     out = {"plain_msm_per_s": plain_rate, "requests": m, "sizes": "log-uniform 2^12..2^22",
            "base_set": nbase, "rates": []}

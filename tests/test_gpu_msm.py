@@ -563,3 +563,30 @@ def test_msm_correctness_from_test_data_files(engine, ref, ocpu, tmp_path):
         ctx.close()
     assert nb == batches
     assert np.array_equal(io.projective_to_affine_records(out), results)
+
+
+@pytest.mark.parametrize("form", ["auto", "windowed"])
+def test_equal_bucket_sums_take_the_complete_formula(engine, ref, ocpu, form):
+    """The reductions add points with the dedicated twisted-Edwards formula, which fails on a
+    doubling; the engine then uses the unified one.  Here every base is the same point P and the
+    scalars are 1..n, so window 0's buckets all hold P: the running sums add equal points
+    (R + B with R = B, A + R with A = R) and the level-2/3 quad sums meet equal run sums.  The
+    second case alternates P and -P under equal scalars, so bucket sums cancel to the identity in
+    a form other than the one the code writes, and the third mixes both with uniform scalars."""
+    n = 4096
+    P = ref.mul(ref.GEN, 0x1234567)
+    same = recs(ref, [P] * n)
+    alt = recs(ref, [P if i % 2 == 0 else ref.neg(P) for i in range(n)])
+    cases = [
+        (same, scal(ref, list(range(1, n + 1)))),
+        (alt, np.repeat(scal(ref, [ref.uniform_scalar(88, 0)]), n, axis=0)),
+        (alt, engine.generate_scalars(89, n)),
+    ]
+    opts = {} if form == "auto" else {"fixed_base": 2}
+    for k, (pts, sc) in enumerate(cases):
+        ctx = engine.multi_scalar_mult_init(pts)
+        try:
+            out = ctx.mult(sc, **opts)
+        finally:
+            ctx.close()
+        assert np.array_equal(out[0], ocpu.msm(pts, sc)), (form, k)
