@@ -919,7 +919,7 @@ def main():
     ap.add_argument("--tune-budget-ms", type=int, default=15000,
                     help="time the batch autotuner may spend on the uneven mix (0: skip it)")
     ap.add_argument("--served-requests", type=int, default=48)
-    ap.add_argument("--served-load", type=float, nargs="*", default=[0.5, 1.5])
+    ap.add_argument("--served-load", type=float, nargs="*", default=[0.5, 1.0, 1.5])
     ap.add_argument("--served-budget-gb", type=int, default=16)
     ap.add_argument("--served-inflight", type=int, nargs="*", default=[2, 4],
                     help="server slots (passes in flight) to sweep at each offered load")

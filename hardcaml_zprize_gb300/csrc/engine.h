@@ -82,6 +82,7 @@ struct PassBuffers {
   uint32_t n_special;
   uint32_t n_classes;
   uint64_t n_bases;             // resident bases (bounds of every base index)
+  uint32_t acc_blocks_per_sm;   // resident k_accumulate blocks per SM (0: 4, the whole SM)
 
   const uint4 *scalars;         // 2 x uint4 per scalar
   const uint4 *host_scalars;    // or null: k_count first copies each scalar from this host buffer

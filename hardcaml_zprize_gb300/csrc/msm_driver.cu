@@ -456,6 +456,7 @@ struct Workspace {
   HostPinned res_host;
   cudaEvent_t ev[MSM_NUM_STAGES + 1] = {};
   uint64_t generation = 0;  // bumps when any buffer moves (graphs must be re-captured)
+  uint32_t acc_blocks_per_sm = 0;  // k_accumulate blocks per SM for this workspace's passes (0: 4)
   struct GraphEntry {
     cudaGraphExec_t exec;
     uint32_t kernels;  // kernel launches in one replay
@@ -499,16 +500,6 @@ struct Workspace {
       graphs.clear();
     }
     return 0;
-  }
-  [[maybe_unused]] void release_sort_buffers() {
-    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
-    graphs.clear();
-    count.release(); offset.release(); fill.release(); taskoff.release(); heavy.release();
-    scan_tmp.release(); vals.release(); tasks.release(); partials.release(); seg_out.release();
-    stage.release(); stage_rank.release(); blk_off.release();
-    order.release(); len_hist.release(); grp_out.release();
-    win_sum.release(); scalars[0].release(); scalars[1].release();
-    generation++;
   }
 };
 
@@ -562,6 +553,7 @@ void set_tables(const Ctx *cx, JobSpec &s) {
 
 PassBuffers make_pass_buffers(Ctx *cx, Workspace &ws, const Plan &pl, const void *d_scalars) {
   PassBuffers pb{};
+  pb.acc_blocks_per_sm = ws.acc_blocks_per_sm;
   pb.bases = cx->bases.as<uint4>();
   pb.flags = cx->flags.as<uint8_t>();
   pb.special_idx = cx->special_idx.as<uint32_t>();
@@ -1176,9 +1168,13 @@ struct Request {
   std::chrono::steady_clock::time_point t_submit, t_done;
 };
 
+// Server passes of at most this many points run on their slot's high-priority stream.
+constexpr uint64_t kServerSmallPass = 1ull << 19;
+
 struct Slot {
   Workspace ws;
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;     // passes of many points, at the lowest stream priority
+  cudaStream_t st_hi = nullptr;  // passes of few points, at the highest
   cudaEvent_t done = nullptr;
   bool busy = false;
   uint64_t bytes = 0;
@@ -1279,6 +1275,10 @@ void Server::loop() {
           for (JobSpec &sp : specs) sp.cfg.seg_len = seg;
         }
         Slot &sl = *free_slot;
+        // a pass of few points goes ahead of a large one: its kernels take SM space first as the
+        // large pass's blocks retire, and the large pass's k_accumulate leaves a quarter of
+        // every SM free for them (slots' workspaces run it with 3 blocks per SM)
+        cudaStream_t st = total_n <= kServerSmallPass ? sl.st_hi : sl.st;
         int rc = build_plan(specs, sl.plan);
         if (!rc && sl.scal.ensure(std::max<uint64_t>(first, 1) * 32) != cudaSuccess)
           rc = fail(ERR_CUDA, "server scalar buffer allocation failed");
@@ -1287,12 +1287,12 @@ void Server::loop() {
           for (auto &r : batch) {
             if (r->n)
               cudaMemcpyAsync((char *)sl.scal.p + off * 32, r->scalars.data(), r->n * 32,
-                              cudaMemcpyHostToDevice, sl.st);
+                              cudaMemcpyHostToDevice, st);
             off += r->n;
           }
-          rc = enqueue_pass(cx, sl.ws, sl.plan, sl.scal.p, sl.st, false, false, 0);
+          rc = enqueue_pass(cx, sl.ws, sl.plan, sl.scal.p, st, false, false, 0);
         }
-        if (!rc) rc = cudaEventRecord(sl.done, sl.st) == cudaSuccess ? 0 : ERR_CUDA;
+        if (!rc) rc = cudaEventRecord(sl.done, st) == cudaSuccess ? 0 : ERR_CUDA;
         if (rc) {
           for (auto &r : batch) {
             r->status = rc;
@@ -1784,15 +1784,27 @@ void *msm_server_create(void *context, uint64_t hbm_budget_bytes, int32_t max_in
   sv->cx = cx;
   sv->budget = hbm_budget_bytes;
   sv->max_inflight = max_inflight;
+  int prio_least = 0, prio_greatest = 0;
+  if (cudaSetDevice(cx->device) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest) != cudaSuccess) {
+    fail(ERR_CUDA, "msm_server_create: stream priorities unavailable");
+    delete sv;
+    return nullptr;
+  }
   for (int i = 0; i < max_inflight; i++) {
     auto sl = std::make_unique<Slot>();
-    if (cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
+    const bool ok =
+        cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, prio_least) == cudaSuccess &&
+        cudaStreamCreateWithPriority(&sl->st_hi, cudaStreamNonBlocking, prio_greatest) == cudaSuccess &&
+        cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) == cudaSuccess;
+    // with passes in flight side by side, k_accumulate leaves room on every SM for the others
+    if (max_inflight > 1) sl->ws.acc_blocks_per_sm = 3;
+    sv->slots.push_back(std::move(sl));
+    if (!ok) {
       fail(ERR_CUDA, "msm_server_create: stream creation failed");
-      delete sv;
+      msm_server_destroy(sv);
       return nullptr;
     }
-    sv->slots.push_back(std::move(sl));
   }
   sv->worker = std::thread([sv] {
     cudaSetDevice(sv->cx->device);
@@ -1860,10 +1872,11 @@ void msm_server_destroy(void *server) {
   sv->cv.notify_all();
   if (sv->worker.joinable()) sv->worker.join();
   for (auto &sl : sv->slots) {
-    if (sl->st) {
-      cudaStreamSynchronize(sl->st);
-      cudaStreamDestroy(sl->st);
-    }
+    for (cudaStream_t x : {sl->st, sl->st_hi})
+      if (x) {
+        cudaStreamSynchronize(x);
+        cudaStreamDestroy(x);
+      }
     if (sl->done) cudaEventDestroy(sl->done);
   }
   delete sv;

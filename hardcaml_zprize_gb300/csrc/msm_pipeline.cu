@@ -1313,7 +1313,7 @@ cudaError_t msm_launch_pass(const PassBuffers &pb, int num_sms, cudaStream_t st,
     launched++;
   }
   mark(4);
-  k_accumulate<<<num_sms * 4, 128, 0, st>>>(pb);
+  k_accumulate<<<num_sms * (pb.acc_blocks_per_sm ? pb.acc_blocks_per_sm : 4), 128, 0, st>>>(pb);
   launched++;
   mark(5);
   k_merge_small<<<num_sms * 4, 128, 0, st>>>(pb);
