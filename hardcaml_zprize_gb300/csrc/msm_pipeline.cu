@@ -607,8 +607,8 @@ __device__ __forceinline__ xyzt_t te_madd_staged(const xyzt_t &p, const uint4 *s
 
 // The first entry of a run starts the sum from the base itself instead of adding it to the
 // identity: x = (y+x)/2 - (y-x)/2, y = (y+x)/2 + (y-x)/2 (x negated for a negative digit), z = 1,
-// t = x y -- one product instead of seven.  The lanes of a warp take their runs together and the
-// runs are nearly equal in length (longest first), so the branch is the same on every lane.
+// t = x y -- one product instead of seven.  The warp fetches its 32 runs together, so every lane
+// is at its run's first entry in the same iteration and the branch is the same on every lane.
 __device__ __forceinline__ xyzt_t te_from_staged(const uint4 *sh, bool neg) {
   const fq_t ymx = staged_fq(sh, 0), ypx = staged_fq(sh, 1);
   xyzt_t r;
