@@ -31,7 +31,6 @@
 namespace {
 
 constexpr uint64_t GL_P = 0xffffffff00000001ull;
-constexpr uint64_t GL_EPS = 0xffffffffull;  // 2^64 mod p
 constexpr uint32_t NTT_MAX_LOG_M = 12;      // longest transform of one block
 constexpr uint32_t NTT_THREADS = 1024;
 
@@ -138,6 +137,7 @@ struct NttPass {
   // twist (pass A): output k of transform g times w_n^(g k mod n), from w_n^e = hi[e >> 12] lo[e & 4095]
   const uint64_t *tw_lo, *tw_hi;
   uint64_t n_mask;  // n - 1 when twisting, 0 otherwise
+  uint64_t scale;   // outputs of an untwisted pass times this (0: none), the inverse's 1/n
 };
 
 __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
@@ -175,6 +175,8 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
     if (ps.n_mask) {
       const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
       v = gl_mul(v, gl_mul(ps.tw_hi[e >> 12], ps.tw_lo[e & 4095]));
+    } else if (ps.scale) {
+      v = gl_mul(v, ps.scale);
     }
     __stcs(ps.dst + (g0 + c) * ps.out_c + (uint64_t)k * ps.out_k, v);
   }
@@ -285,6 +287,8 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass8(NttPass ps) {
     if (ps.n_mask) {
       const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
       v = gl_mul(v, gl_mul(ps.tw_hi[e >> 12], ps.tw_lo[e & 4095]));
+    } else if (ps.scale) {
+      v = gl_mul(v, ps.scale);
     }
     __stcs(ps.dst + (g0 + c) * ps.out_c + (uint64_t)k * ps.out_k, v);
   }
@@ -334,6 +338,8 @@ struct NttCtx {
   // moves by a copy kernel instead of a driver copy
   bool host_direct = false;
   bool radix2 = false;  // the radix-2 pass kernel (comparison)
+  bool inverse = false;   // roots w^-1 and outputs times 1/n
+  uint64_t scale_single = 0;  // 1/n for an inverse of one pass (the twist carries it otherwise)
   int num_sms = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev[5] = {};
@@ -356,6 +362,19 @@ struct NttCtx {
   }
 };
 
+uint64_t h_pow(uint64_t b, uint64_t e) {
+  uint64_t r = 1;
+  for (; e; e >>= 1, b = h_mul(b, b))
+    if (e & 1) r = h_mul(r, b);
+  return r;
+}
+uint64_t h_inv(uint64_t a) { return h_pow(a, GL_P - 2); }  // Fermat; a != 0
+
+// the 2^k-th root the context transforms with: the reference's, or its inverse
+uint64_t ctx_root(const NttCtx *cx, uint32_t k) {
+  return cx->inverse ? h_inv(GL_OMEGA[k]) : GL_OMEGA[k];
+}
+
 // w^0 .. w^(count - 1)
 std::vector<uint64_t> powers(uint64_t w, uint64_t count) {
   std::vector<uint64_t> v(std::max<uint64_t>(count, 1));
@@ -377,7 +396,7 @@ size_t pass_smem(uint32_t log_m, uint32_t cols) {
 // one pass: `count` transforms of 2^log_m points, `cols` per block
 cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, uint32_t log_m,
                         uint64_t count, uint64_t in_c, uint64_t in_i, uint64_t out_c, uint64_t out_k,
-                        const uint64_t *tw_m, bool twist, cudaStream_t st) {
+                        const uint64_t *tw_m, bool twist, cudaStream_t st, uint64_t scale = 0) {
   NttPass ps;
   ps.src = src;
   ps.dst = dst;
@@ -391,6 +410,7 @@ cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, ui
   ps.tw_lo = cx->d_twlo;
   ps.tw_hi = cx->d_twhi;
   ps.n_mask = twist ? cx->n - 1 : 0;
+  ps.scale = twist ? 0 : scale;
   const uint32_t blocks = (uint32_t)(count / ps.cols);
   const uint32_t threads = std::min<uint32_t>(NTT_THREADS, std::max<uint32_t>(32, ps.cols << (log_m - (log_m ? 1 : 0))));
   if (cx->radix2)
@@ -403,7 +423,8 @@ cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, ui
 // the transform of cx->n points from d_src to d_dst (device memory), enqueued on st
 int enqueue_ntt(NttCtx *cx, uint64_t *d_dst, const uint64_t *d_src, cudaStream_t st, bool marks) {
   if (cx->log_n <= NTT_MAX_LOG_M) {
-    NCK(launch_pass(cx, d_src, d_dst, cx->log_n, 1, 0, 1, 0, 1, cx->d_tw1, false, st));
+    NCK(launch_pass(cx, d_src, d_dst, cx->log_n, 1, 0, 1, 0, 1, cx->d_tw1, false, st,
+                    cx->scale_single));
     if (marks) NCK(cudaEventRecord(cx->ev[2], st));
     return 0;
   }
@@ -428,13 +449,19 @@ int ntt_last_error(char *buf, size_t len) {
   return g_err;
 }
 
-void *ntt_init(uint32_t log_n) {
+}  // extern "C"
+
+namespace {
+
+// a context of either direction (ntt_init, ntt_init_inverse)
+void *ntt_create(uint32_t log_n, bool inverse) {
   g_err = 0;
   if (log_n > 2 * NTT_MAX_LOG_M) {
     fail(NTT_ERR_ARG, "ntt_init: 2^%u points is over the maximum of 2^%u", log_n, 2 * NTT_MAX_LOG_M);
     return nullptr;
   }
   auto *cx = new NttCtx();
+  cx->inverse = inverse;
   const char *dev = getenv("MSM_DEVICE");
   cx->device = dev ? atoi(dev) : 0;
   if (const char *c = getenv("NTT_COLS")) {  // transforms per block: 1, 2 or 4
@@ -470,16 +497,24 @@ void *ntt_init(uint32_t log_n) {
   step(cudaMalloc(&cx->d_out, cx->n * 8), "output buffer");
   if (log_n > NTT_MAX_LOG_M) step(cudaMalloc(&cx->d_tmp, cx->n * 8), "intermediate buffer");
   if (!rc) {
-    // short-transform roots: w_m = w_n^(n/m), from the reference's table
+    // short-transform roots: w_m = w_n^(n/m), from the reference's table (inverted for the
+    // inverse transform)
     const uint32_t l1 = log_n > NTT_MAX_LOG_M ? cx->log_n1 : log_n;
-    rc = upload(&cx->d_tw1, powers(GL_OMEGA[l1], (1ull << l1) / 2));
+    rc = upload(&cx->d_tw1, powers(ctx_root(cx, l1), (1ull << l1) / 2));
+    // the inverse's 1/n: in the twist of pass A (every entry of the high table), or in the
+    // store of a transform of one pass
+    const uint64_t inv_n = h_inv(cx->n % GL_P);
+    if (inverse && log_n <= NTT_MAX_LOG_M) cx->scale_single = inv_n;
     if (!rc && log_n > NTT_MAX_LOG_M) {
-      rc = upload(&cx->d_tw2, powers(GL_OMEGA[cx->log_n2], (1ull << cx->log_n2) / 2));
-      const uint64_t w = GL_OMEGA[log_n];
+      rc = upload(&cx->d_tw2, powers(ctx_root(cx, cx->log_n2), (1ull << cx->log_n2) / 2));
+      const uint64_t w = ctx_root(cx, log_n);
       if (!rc) rc = upload(&cx->d_twlo, powers(w, std::min<uint64_t>(cx->n, 4096)));
       uint64_t w4096 = w;
       for (int i = 0; i < 12; i++) w4096 = h_mul(w4096, w4096);
-      if (!rc) rc = upload(&cx->d_twhi, powers(w4096, std::max<uint64_t>(cx->n >> 12, 1)));
+      std::vector<uint64_t> hi = powers(w4096, std::max<uint64_t>(cx->n >> 12, 1));
+      if (inverse)
+        for (uint64_t &v : hi) v = h_mul(v, inv_n);
+      if (!rc) rc = upload(&cx->d_twhi, hi);
     }
   }
   if (rc) {
@@ -488,6 +523,14 @@ void *ntt_init(uint32_t log_n) {
   }
   return cx;
 }
+
+}  // namespace
+
+extern "C" {
+
+void *ntt_init(uint32_t log_n) { return ntt_create(log_n, false); }
+
+void *ntt_init_inverse(uint32_t log_n) { return ntt_create(log_n, true); }
 
 void ntt_free(void *context) { delete (NttCtx *)context; }
 

@@ -16,9 +16,9 @@ import numpy as np
 from . import MsmError, load_library
 
 GL_P = 0xFFFFFFFF00000001
-EXPORTED = ["ntt_init", "ntt_input_vector_size", "ntt_evaluate", "ntt_evaluate_device",
-            "ntt_last_timings", "ntt_last_error", "ntt_free", "ntt_field_selftest",
-            "ntt_evaluate_batch"]
+EXPORTED = ["ntt_init", "ntt_init_inverse", "ntt_input_vector_size", "ntt_evaluate",
+            "ntt_evaluate_device", "ntt_last_timings", "ntt_last_error", "ntt_free",
+            "ntt_field_selftest", "ntt_evaluate_batch"]
 NTT_STAGES = ["h2d", "pass_a", "pass_b", "d2h"]
 
 _declared = False
@@ -31,6 +31,7 @@ def _lib():
         P, U64, I32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32
         sig = {
             "ntt_init": (P, [ctypes.c_uint32]),
+            "ntt_init_inverse": (P, [ctypes.c_uint32]),
             "ntt_input_vector_size": (U64, [P]),
             "ntt_evaluate": (ctypes.c_int, [P, P, P, U64]),
             "ntt_evaluate_device": (ctypes.c_int, [P, P, P, P]),
@@ -65,12 +66,15 @@ def field_selftest(op: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:
 
 
 class NttContext:
-    """Transforms of 2^log_n points (log_n <= 24) with device buffers allocated once."""
+    """Transforms of 2^log_n points (log_n <= 24) with device buffers allocated once.  With
+    inverse=True the context computes the inverse transform, x[j] = (1/n) sum_k X[k] w^(-j k)
+    (ntt_init_inverse)."""
 
-    def __init__(self, log_n: int):
-        self.handle = _lib().ntt_init(log_n)
+    def __init__(self, log_n: int, inverse: bool = False):
+        self.handle = (_lib().ntt_init_inverse if inverse else _lib().ntt_init)(log_n)
         if not self.handle:
             raise MsmError(f"ntt_init: {last_error()}")
+        self.inverse = inverse
         self.log_n = log_n
         self.n = 1 << log_n
 

@@ -28,6 +28,13 @@ extern "C" {
  * (driver.h:158-170; host/driver.cpp).  Returns NULL on failure (ntt_last_error says why). */
 void *ntt_init(uint32_t log_n);
 
+/* A context for the inverse transform of 2^log_n points: x[j] = (1/n) sum_k X[k] w^(-j k), so
+ * that it undoes ntt_evaluate of an ntt_init context of the same size.  Every other entry point
+ * takes it unchanged.  The FPGA computes one direction only; the reference's software model
+ * holds both (libs/hardcaml_ntt/src/reference_model.ml:6-55, forward_dit with the other root
+ * table) and its round-trip test scales by 1/n (libs/hardcaml_ntt/test/test_ntt_roundtrip.ml:7-23). */
+void *ntt_init_inverse(uint32_t log_n);
+
 /* Number of elements of one transform (NttFpgaDriver::input_vector_size, driver.h:160). */
 uint64_t ntt_input_vector_size(void *context);
 

@@ -139,3 +139,42 @@ def test_batch_equals_single_calls(ntt_mod, ocpu):
         assert np.array_equal(again, got[:3])
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("log_n", [0, 1, 2, 5, 12, 13, 17, 20])
+def test_inverse_ntt_matches_oracle(ntt_mod, ocpu, log_n):
+    """ntt_init_inverse against the oracle's inverse (root w^-1, scaled by 1/n), on one pass
+    (log_n <= 12) and on two (the 1/n rides in the twist)."""
+    rng = np.random.default_rng(300 + log_n)
+    x = random_below_p(rng, 1 << log_n)
+    x[0] = P - 1
+    ctx = ntt_mod.NttContext(log_n, inverse=True)
+    try:
+        assert ctx.input_vector_size() == 1 << log_n
+        assert np.array_equal(ctx.evaluate(x), ocpu.ntt(x, inverse=True))
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("log_n", [12, 24])
+def test_round_trip_at_full_size(ntt_mod, log_n):
+    """Forward then inverse on device buffers gives the input back (the reference model's
+    round-trip property, libs/hardcaml_ntt/test/test_ntt_roundtrip.ml), at 2^24 too."""
+    import torch
+
+    rng = np.random.default_rng(400 + log_n)
+    x = random_below_p(rng, 1 << log_n)
+    fwd, inv = ntt_mod.NttContext(log_n), ntt_mod.NttContext(log_n, inverse=True)
+    try:
+        d_x = torch.from_numpy(x.view(np.int64)).cuda()
+        d_y, d_z = torch.empty_like(d_x), torch.empty_like(d_x)
+        torch.cuda.synchronize()
+        st = torch.cuda.Stream()  # one stream orders the two contexts' transforms
+        fwd.evaluate_device(d_y.data_ptr(), d_x.data_ptr(), st.cuda_stream)
+        inv.evaluate_device(d_z.data_ptr(), d_y.data_ptr(), st.cuda_stream)
+        torch.cuda.synchronize()
+        assert not np.array_equal(d_y.cpu().numpy(), d_x.cpu().numpy())
+        assert np.array_equal(d_z.cpu().numpy().view(np.uint64), x)
+    finally:
+        fwd.close()
+        inv.close()

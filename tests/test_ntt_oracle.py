@@ -63,6 +63,19 @@ def test_oracle_matches_definition(ocpu, logn):
     assert [int(t) for t in ocpu.ntt(np.array(x, dtype=np.uint64))] == dft(x, logn)
 
 
+@pytest.mark.parametrize("logn", [0, 1, 2, 3, 5, 7])
+def test_oracle_inverse_matches_definition(ocpu, logn):
+    """The oracle's inverse, x[j] = (1/n) sum_k X[k] w^(-j k), which the GPU's ntt_init_inverse is
+    checked against (the reference model's transform with the other root table,
+    libs/hardcaml_ntt/src/reference_model.ml:54-55, scaled as its round-trip test scales)."""
+    rng = random.Random(50 + logn)
+    n = 1 << logn
+    X = [rng.randrange(P) for _ in range(n)]
+    winv, ninv = pow(ocpu.gl_omega(logn), P - 2, P), pow(n, P - 2, P)
+    want = [sum(X[k] * pow(winv, j * k, P) for k in range(n)) * ninv % P for j in range(n)]
+    assert [int(t) for t in ocpu.ntt(np.array(X, dtype=np.uint64), inverse=True)] == want
+
+
 def test_all_ones_and_roundtrip(ocpu):
     n = 1 << 12
     out = ocpu.ntt(np.ones(n, dtype=np.uint64))
