@@ -187,7 +187,10 @@ typedef struct {
 } msm_server_stats_t;
 
 /* `hbm_budget_bytes` bounds the device memory of scalar/sort/bucket buffers of passes in
- * flight; `max_inflight` bounds concurrent passes (each on its own stream). */
+ * flight; `max_inflight` bounds concurrent passes (each slot has a stream at the lowest and one
+ * at the highest priority: a pass of at most 2^19 points takes the high one, and with more than
+ * one slot every pass's accumulation leaves a quarter of each SM free, so small requests do not
+ * wait for a large pass to finish). */
 void *msm_server_create(void *context, uint64_t hbm_budget_bytes, int32_t max_inflight);
 /* Copy the request's scalars and queue it; returns its id (>= 0) or a negative error. */
 int64_t msm_server_submit(void *server, const biginteger256_t *scalars, uint64_t n,
