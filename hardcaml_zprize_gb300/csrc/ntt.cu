@@ -226,25 +226,31 @@ __device__ __forceinline__ void dif_round(const NttPass &ps, uint64_t *sm, uint3
   const uint32_t m = 1u << ps.log_m, C = ps.cols, units = m >> R;
   const uint64_t g0 = (uint64_t)blockIdx.x * C;
   const bool c_fast = from_global && ps.in_c == 1;  // consecutive lanes on consecutive transforms
+  // q0 holds no bit of t << log_hmin, so q = q0 ^ (t << log_hmin), and the swizzle is linear over
+  // XOR: slot(q) = slot(q0) ^ slot(t << log_hmin), the second term fixed for the round
+  uint32_t st[1 << R];
+#pragma unroll
+  for (int t = 0; t < (1 << R); t++) st[t] = slot((uint32_t)t << log_hmin);
   for (uint32_t w = threadIdx.x; w < C * units; w += blockDim.x) {
     const uint32_t c = c_fast ? w % C : w / units, u = c_fast ? w / C : w % units;
     const uint32_t j = u & ((1u << log_hmin) - 1), b = u >> log_hmin;
     const uint32_t q0 = (b << (log_hmin + R)) + j;
+    const uint32_t s0 = slot(q0);
     uint64_t x[8];
     uint64_t *a = sm + (size_t)c * pitch;
 #pragma unroll
     for (int t = 0; t < (1 << R); t++) {
-      const uint32_t q = q0 + ((uint32_t)t << log_hmin);
       if (from_global) {
+        const uint32_t q = q0 + ((uint32_t)t << log_hmin);
         uint64_t v = __ldcs(ps.src + (g0 + c) * ps.in_c + (uint64_t)q * ps.in_i);
         x[t] = v >= GL_P ? v - GL_P : v;  // inputs are taken modulo p
       } else {
-        x[t] = a[slot(q)];
+        x[t] = a[s0 ^ st[t]];
       }
     }
     dif_unit<R, LAST>(x, j, log_hmin, ps.log_m, tw);
 #pragma unroll
-    for (int t = 0; t < (1 << R); t++) a[slot(q0 + ((uint32_t)t << log_hmin))] = x[t];
+    for (int t = 0; t < (1 << R); t++) a[s0 ^ st[t]] = x[t];
   }
 }
 
