@@ -130,7 +130,8 @@ struct NttPass {
   const uint64_t *src;
   uint64_t *dst;
   uint32_t log_m;  // transform length of this pass
-  uint32_t cols;   // transforms per block (1..4)
+  uint32_t cols;   // transforms per block (1, 2 or 4)
+  uint32_t log_cols;  // log2 cols: the block's index splits are shifts and masks, not divisions
   uint64_t in_c, in_i;    // element i of transform g: src[g in_c + i in_i]
   uint64_t out_c, out_k;  // output k of transform g: dst[g out_c + k out_k]
   const uint64_t *tw_m;   // w_m^j, j < m/2
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
   // load C transforms, element i to its bit-reversed slot; the unit-stride index runs fastest
   const bool c_fast = ps.in_c == 1;
   for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
-    const uint32_t c = c_fast ? t % C : t / m, i = c_fast ? t / C : t % m;
+    const uint32_t c = c_fast ? t & (C - 1) : t >> ps.log_m, i = c_fast ? t >> ps.log_cols : t & (m - 1);
     uint64_t v = __ldcs(ps.src + (g0 + c) * ps.in_c + (uint64_t)i * ps.in_i);
     if (v >= GL_P) v -= GL_P;  // inputs are taken modulo p
     sm[(size_t)c * m + bit_reverse(i, ps.log_m)] = v;
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass(NttPass ps) {
   }
   // store, output groups of C consecutive transforms together
   for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
-    const uint32_t c = t % C, k = t / C;
+    const uint32_t c = t & (C - 1), k = t >> ps.log_cols;
     uint64_t v = sm[(size_t)c * m + k];
     if (ps.n_mask) {
       const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
@@ -232,7 +233,8 @@ __device__ __forceinline__ void dif_round(const NttPass &ps, uint64_t *sm, uint3
 #pragma unroll
   for (int t = 0; t < (1 << R); t++) st[t] = slot((uint32_t)t << log_hmin);
   for (uint32_t w = threadIdx.x; w < C * units; w += blockDim.x) {
-    const uint32_t c = c_fast ? w % C : w / units, u = c_fast ? w / C : w % units;
+    const uint32_t c = c_fast ? w & (C - 1) : w >> (ps.log_m - R);
+    const uint32_t u = c_fast ? w >> ps.log_cols : w & (units - 1);
     const uint32_t j = u & ((1u << log_hmin) - 1), b = u >> log_hmin;
     const uint32_t q0 = (b << (log_hmin + R)) + j;
     const uint32_t s0 = slot(q0);
@@ -288,7 +290,7 @@ __global__ void __launch_bounds__(NTT_THREADS) k_ntt_pass8(NttPass ps) {
   }
   // gather in natural order, output groups of C consecutive transforms together
   for (uint32_t t = threadIdx.x; t < C * m; t += blockDim.x) {
-    const uint32_t c = t % C, k = t / C;
+    const uint32_t c = t & (C - 1), k = t >> ps.log_cols;
     uint64_t v = sm[(size_t)c * pitch + slot(bit_reverse(k, ps.log_m))];
     if (ps.n_mask) {
       const uint64_t e = ((g0 + c) * (uint64_t)k) & ps.n_mask;
@@ -407,7 +409,8 @@ cudaError_t launch_pass(const NttCtx *cx, const uint64_t *src, uint64_t *dst, ui
   ps.src = src;
   ps.dst = dst;
   ps.log_m = log_m;
-  ps.cols = (uint32_t)std::min<uint64_t>(cx->cols, count);
+  ps.cols = (uint32_t)std::min<uint64_t>(cx->cols, count);  // powers of two
+  ps.log_cols = (uint32_t)__builtin_ctz(ps.cols);
   ps.in_c = in_c;
   ps.in_i = in_i;
   ps.out_c = out_c;
