@@ -7,11 +7,15 @@
 //   pass A: for every column j1 of the n2 x n1 row-major input, the n2-point transform over j2,
 //           times w^(j1 k2), written to Z[k2][j1];
 //   pass B: for every row k2 of Z, the n1-point transform over j1, written to X[k2 + n2 k1].
-// One kernel does both passes: a block loads C <= 4 of the short transforms into shared memory
-// (bit-reversed positions), runs the log2(m) radix-2 decimation-in-time stages there, and stores
-// them, optionally twisted.  With C = 4 every row of a column load and every output group of a
-// store is 32 contiguous bytes, one DRAM sector.  HBM traffic: n x 8 B read and written per pass.
-// Transforms of at most 2^12 points are one pass.
+// One kernel (k_ntt_pass8) does both passes: a block holds C <= 4 of the short transforms in
+// shared memory, runs them as radix-8 decimation-in-frequency rounds (three stages per round in
+// registers), and gathers the outputs in natural order, optionally twisted.  With C = 4 every row
+// of a column load and every output group of a store is 32 contiguous bytes, one DRAM sector.
+// HBM traffic: n x 8 B read and written per pass.  k_ntt_pass, the first form (radix-2
+// decimation-in-time stages on bit-reversed positions), stays for comparison (NTT_RADIX2=1).
+// Transforms of at most 2^12 points are one pass.  An inverse context (ntt_init_inverse) runs the
+// same kernels with the inverse roots and multiplies by 1/n: the factor sits in pass A's twist
+// table, or in the store of a transform of one pass.
 //
 // Field arithmetic: elements in [0, p).  The 128-bit product hi 2^64 + lo reduces with
 // 2^64 = 2^32 - 1 and 2^96 = -1 (mod p): hi = hh 2^32 + hl gives lo - hh + hl (2^32 - 1).
@@ -87,7 +91,8 @@ __device__ __forceinline__ uint64_t gl_sub(uint64_t a, uint64_t b) {
 
 // a b: the 128-bit product (r3 r2 r1 r0) from four wide multiplies whose 64-bit addends carry
 // the partial products' overflow (the carries ride in the multiplies, which run on the multiply
-// pipe; the passes are bound by the integer ALU pipe), then lo + hl (2^32 - 1) - hh with
+// pipe, and not in add chains on the integer ALU, which bounded the passes), then
+// lo + hl (2^32 - 1) - hh with
 // lo = r1 r0, hl = r2, hh = r3 (2^64 = 2^32 - 1, 2^96 = -1 mod p): hl (2^32 - 1) is a fifth wide
 // multiply, each step is corrected by its own carry or borrow, and a last conditional
 // subtraction of p makes the value canonical.
