@@ -8,11 +8,13 @@
 //                  without a stage)
 //   4. k_tasks     split every bucket into runs of <= seg_len entries (load balance under skew)
 //   5. k_accumulate persistent: each thread sums one run of bases into a partial bucket sum
+//                  (the run's first base taken as is, then a 7-product mixed add per base)
 //   6. k_merge_*   buckets split over several runs: sum of their partials (a thread, a warp or
 //                  a block per bucket, by the number of runs)
-//   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33)
+//   7. k_reduce1   per run of buckets: running sum R and triangle sum A (pippenger.h:25-33),
+//                  by the dedicated addition (8 products; the unified one where it fails)
 //   8. k_reduce2/3 combine runs into groups, groups into window sums (k_reduce3_small: one
-//                  quad per window of few groups)
+//                  quad per window of few groups), by quad additions of two product latencies
 //   9. k_final     per MSM: Horner window combine (pippenger.h:36-45), map back to affine
 //                  Weierstrass, add the bases without a twisted-Edwards image
 //                  (driver.cpp:349-372), write g1_projective_t (bls12_377_g1.h:427-439, 667-690)
