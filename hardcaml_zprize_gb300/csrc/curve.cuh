@@ -131,6 +131,9 @@ __device__ __forceinline__ xyzt_t te_add_fast(const xyzt_t &p, const xyzt_t &q) 
   r.z = fq_mul_nv(F, G);
   return r;
 }
+static __device__ __noinline__ xyzt_t te_add_fast_ool(const xyzt_t &p, const xyzt_t &q) {
+  return te_add_fast(p, q);
+}
 
 // small scalar multiple k*p (k >= 0) by double-and-add from the top bit
 static __device__ __noinline__ xyzt_t te_mul_small(const xyzt_t &p, uint32_t k) {

@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(128) k_merge_small(PassBuffers pb) {
     for (uint32_t k = 1; k < nt; k++) {
       xyzt_t p;
       xyzt_load(p, pb.partials + (size_t)(t0 + k) * 12);
-      acc = te_add_ool(acc, p);
+      acc = te_add_fast_ool(acc, p);  // partials of disjoint runs: the dedicated formula
     }
     xyzt_store(pb.partials + (size_t)t0 * 12, acc);
   }
