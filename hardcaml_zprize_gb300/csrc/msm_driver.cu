@@ -533,6 +533,8 @@ struct Ctx {
   // a shared pass overlaps the serial tails of its MSMs, so the best form can differ from the
   // best for one MSM alone
   std::map<uint32_t, Cfg> tuned_batch;
+  // guards tuned and tuned_batch: a server's worker reads them while a tuner may write them
+  std::mutex tune_mu;
   ~Ctx() {
     if (stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -677,11 +679,15 @@ int check_pass_errors(Workspace &ws, cudaStream_t st, uint64_t *stats_out) {
 Cfg resolve_cfg(Ctx *cx, uint64_t n, const msm_options_t *opt, bool shared_pass = false) {
   Cfg cfg = heuristic_cfg(n);
   const uint32_t cls = log2_ceil(std::max<uint64_t>(n, 1));
-  const std::map<uint32_t, Cfg> &tmap =
-      shared_pass && cx->tuned_batch.count(cls) ? cx->tuned_batch : cx->tuned;
-  auto it = tmap.find(cls);
-  const bool tuned = it != tmap.end();
-  if (tuned) cfg = it->second;
+  bool tuned = false;
+  {
+    std::lock_guard<std::mutex> lk(cx->tune_mu);
+    const std::map<uint32_t, Cfg> &tmap =
+        shared_pass && cx->tuned_batch.count(cls) ? cx->tuned_batch : cx->tuned;
+    auto it = tmap.find(cls);
+    tuned = it != tmap.end();
+    if (tuned) cfg = it->second;
+  }
   const bool forced_c = opt && opt->window_bits > 0;
   if (opt) {
     if (forced_c) {
@@ -1565,7 +1571,10 @@ int msm_tune(void *context, uint64_t npoints, int32_t budget_ms, msm_options_t *
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cx->tuned[log2_ceil(npoints)] = best;
+  {
+    std::lock_guard<std::mutex> lk(cx->tune_mu);
+    cx->tuned[log2_ceil(npoints)] = best;
+  }
   if (const char *path = getenv("MSM_TUNE_CACHE")) {
     if (FILE *f = fopen(path, "a")) {
       fprintf(f, "%u %u %u %u %u %.4f %u\n", log2_ceil(npoints), best.c, best.signed_digits,
@@ -1736,7 +1745,10 @@ int msm_tune_uneven(void *context, uint64_t num_msms, const uint64_t *sizes,
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  for (auto &kv : form) cx->tuned_batch[kv.first] = kv.second;
+  {
+    std::lock_guard<std::mutex> lk(cx->tune_mu);
+    for (auto &kv : form) cx->tuned_batch[kv.first] = kv.second;
+  }
   if (const char *path = getenv("MSM_TUNE_CACHE")) {
     if (FILE *f = fopen(path, "a")) {
       for (auto &kv : form)
