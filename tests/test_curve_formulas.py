@@ -20,7 +20,7 @@ Q = b.Q
 
 
 def dedicated(p1, p2):
-    """add-2008-hwcd-4 with a = -1, in the order the device computes it (curve.cuh te_add_ded)."""
+    """add-2008-hwcd-4 with a = -1, in the order the device computes it (curve.cuh te_add_fast)."""
     X1, Y1, Z1, T1 = p1
     X2, Y2, Z2, T2 = p2
     A = (Y1 - X1) * (Y2 + X2) % Q
